@@ -1,0 +1,332 @@
+"""Benchmark: particle-steps/s of the GB300 DEM step engine.
+
+Default workload: the single large system (3D bidisperse spheres,
+N = 1,048,576, radii 0.5/0.7, periodic box at packing fraction 0.55,
+linear spring k = 1e3, velocity Verlet, dt = 5e-4), synthetic and seeded.
+
+  value     particle-steps/s with the state resident in HBM, CUDA events on
+            the engine's stream around graph-captured 50-step chunks; L2 is
+            flushed (256 MB write) between timed chunks.
+  e2e       the same metric through the C ABI with host buffers: pinned host
+            upload, K steps, host download inside the timed region.
+  roofline  the fused force/integrate kernel: 80 B per particle-step (3D
+            state record read + write) over its average launch duration,
+            measured in an instrumented pass with per-launch CUDA events.
+  cpu_baseline  the C/OpenMP restatement of the reference step on the host
+            cores, on a bounded sample of steps of the same workload.
+
+``--impl reference`` times that CPU restatement alone (the reference is a
+JAX program that cannot be installed here).  Under torchrun with N > 1 each
+rank runs an independent replica (the path has no exchange step).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_PARTICLE_STEP = {3: 80, 2: 56}
+CHUNK = 50
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    p.add_argument("--skin", type=float, default=None)
+    p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def make_workload(name, n, rank):
+    from jaxdem_gb300 import workloads as W
+
+    seed_off = 1000 * rank
+    if name == "c1":
+        return W.c1(**({"N": n} if n else {}), seed=1 + seed_off)
+    if name == "c2":
+        return W.c2(**({"N": n} if n else {}), seed=2 + seed_off)
+    return W.c3(**({"N": n} if n else {}), seed=3 + seed_off)
+
+
+def describe(w):
+    return {
+        "c1": "3D monodisperse spheres N={N} r=0.5 periodic phi=0.40 dt=1e-3",
+        "c2": "3D bidisperse spheres N={N} r=0.5/0.7 periodic phi=0.55 dt=5e-4",
+        "c3": "2D polydisperse disks N={N} r~U[0.4,0.6] reflect phi=0.70 gravity -y dt=5e-4",
+    }[w.name].format(N=w.N)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        exe = shutil.which("nvidia-smi")
+        if not exe:
+            return
+        self.proc = subprocess.Popen([exe, f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits", "-lms", "100"],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+
+        self.th = threading.Thread(target=rd, daemon=True)
+        self.th.start()
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_baseline(w, seconds, max_steps=1000):
+    """C/OpenMP restatement of the reference step on the host cores."""
+    import oracle
+
+    threads = oracle.max_threads()
+    pos, vel, frc = w.pos.copy(), w.vel.copy(), np.zeros_like(w.pos)
+    kw = dict(domain=w.domain, box=w.box_size, anchor=w.anchor, dt=w.dt, cell_size=2 * float(w.rad.max()),
+              gravity=w.gravity, restitution=w.restitution, threads=threads)
+    oracle.c_step(w.dim, pos, vel, frc, w.rad, w.mass, steps=1, **kw)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        oracle.c_step(w.dim, pos, vel, frc, w.rad, w.mass, steps=1, **kw)
+        steps += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": w.N * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the same {w.N}-particle workload (C/OpenMP restatement of the "
+                      f"reference step, float32), {dt:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = make_workload(args.workload, args.n, 0)
+    per_step = []
+    for _ in range(args.warmup):
+        cpu_baseline(w, seconds=0.0, max_steps=1)
+    res = cpu_baseline(w, seconds=max(5.0, args.cpu_seconds), max_steps=max(args.steps, 1))
+    val = res["value"]
+    line = {"metric": "particle-steps/s", "value": val, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": w.N / val * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": describe(w), "N": w.N},
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": res["cores"], "kind": res["kind"],
+                             "sample": res["sample"]},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------- ours
+def traffic_from_profile(workload):
+    """dram bytes per fused-kernel launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d.get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+
+    from jaxdem_gb300 import workloads as W
+    from jaxdem_gb300._lib import Engine, host_register, host_unregister
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = make_workload(args.workload, args.n, rank)
+    skin = args.skin if args.skin is not None else 0.1 * float(w.rad.max())
+    young = np.array([[W.K_SPRING]], np.float32)
+    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
+    eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    # warm-up steps (graph capture, first re-sort)
+    for _ in range(max(args.warmup, 1)):
+        eng.step(1)
+    eng.step(CHUNK)
+
+    K = args.steps
+    chunks = [CHUNK] * (K // CHUNK) + ([K % CHUNK] if K % CHUNK else [])
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    total_ms = 0.0
+    for c in chunks:
+        flush.fill_(float(c))
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        eng.step_async(c)
+        e.record(stream)
+        e.synchronize()
+        total_ms += s.elapsed_time(e)
+    eng.sync()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    stats = eng.stats()
+
+    # instrumented pass: per-launch events around the fused force kernel
+    tot_ms, force_ms = eng.step_timed(CHUNK)
+    force_avg_ms = force_ms / CHUNK
+    B = BYTES_PER_PARTICLE_STEP[w.dim]
+    peak, peak_kind = peaks()
+    achieved = B * w.N / (force_avg_ms * 1e-3) / 1e9
+    traffic = traffic_from_profile(args.workload)
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = {k: np.ascontiguousarray(getattr(w, k).copy()) for k in ("pos", "vel", "rad", "mass")}
+        outb = {"pos_c": np.empty_like(w.pos), "vel": np.empty_like(w.vel), "force": np.empty_like(w.pos)}
+        for a in list(host.values()) + list(outb.values()):
+            host_register(a)
+        e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
+        e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
+        e2e_eng.step(CHUNK)  # capture graphs once, outside the timed region
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
+        e2e_eng.step(K)
+        e2e_eng.download(outb)
+        e2e_s = time.perf_counter() - t0
+        for a in list(host.values()) + list(outb.values()):
+            host_unregister(a)
+        e2e_eng.close()
+        h2d = sum(a.nbytes for a in host.values())
+        d2h = sum(a.nbytes for a in outb.values())
+        e2e = {"value": world * w.N * K / e2e_s, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+               "note": f"one C-ABI call sequence per {K} steps: upload (pinned host), step, download"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.cpu_seconds)
+
+    value = world * w.N * K / (total_ms * 1e-3)
+    n_launch_per_call = 1 + 8  # pre + per step: 7 re-sort kernels (return early when not due) + fused step
+    launches = sum(1 + 8 * c for c in chunks)
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": describe(w), "N": w.N, "skin": skin, "chunk_steps": CHUNK,
+                   "l2": "flushed (256 MB write) between timed 50-step chunks",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "rebuilds_in_run": stats["rebuilds"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_force (fused force + integrate)", "bytes_per_unit": B,
+                     "avg_launch_ms": force_avg_ms},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        if args.impl == "ours":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            tdist.init_process_group("nccl")
+            dist = tdist
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import __graft_entry__ as g
+
+    g.build()
+    run_ours(args, rank, world, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

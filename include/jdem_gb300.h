@@ -1,0 +1,195 @@
+/*
+ * jdem_gb300 -- C ABI of the GB300 DEM step engine.
+ *
+ * The engine replaces JaxDEM's per-step hot path (paths relative to the
+ * JaxDEM project):
+ *   System.step / _step_once           jaxdem/system.py:60-98, 701-748
+ *   DynamicCellList.compute_force      jaxdem/colliders/cell_list.py:434-464
+ *   DynamicCellList.compute_potential_energy  jaxdem/colliders/cell_list.py:466-496
+ *   SpringForce.force / energy         jaxdem/forces/spring.py:69-147
+ *   ForceManager.apply (gravity)       jaxdem/forces/force_manager.py:338-425
+ *   VelocityVerlet before/after        jaxdem/integrators/velocity_verlet.py:29-95
+ *   DirectEuler after                  jaxdem/integrators/direct_euler.py:30-66
+ *   VelocityVerletSpiral / Spiral      jaxdem/integrators/velocity_verlet_spiral.py:36-180,
+ *                                      jaxdem/integrators/spiral.py
+ *   Periodic / Reflect / Free domains  jaxdem/domains/periodic.py:74-79,
+ *                                      jaxdem/domains/reflect.py:99-299, _toc.py:11-94,
+ *                                      jaxdem/domains/free.py:40-63
+ * JaxDEM itself has no native FFI; these entry points are what a JAX FFI
+ * custom call (or the ctypes binding shipped in jaxdem_gb300/_lib.py) binds.
+ *
+ * Conventions.  Every function returns an int status (JDEM_OK = 0).  No C++
+ * exception crosses this boundary.  A handle owns its device memory, which
+ * stays resident between calls; host buffers belong to the caller.  All work
+ * is ordered on the handle's stream.  A handle is not internally locked: use
+ * one handle per host thread.  Arrays use the reference's row-major layouts:
+ * pos_c/vel/force (N, dim), q (N, 4) as (w, x, y, z), ang_vel/torque/inertia
+ * (N, 1) in 2D or (N, 3) in 3D, bond_id (N, W) padded with -1.  With several
+ * systems in one handle their particles are concatenated in system order.
+ */
+#ifndef JDEM_GB300_H
+#define JDEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JDEM_ABI_VERSION 1
+
+enum {
+  JDEM_OK = 0,
+  JDEM_ERR_BAD_ARG = 1,
+  JDEM_ERR_CAPACITY_OVERFLOW = 2,
+  JDEM_ERR_HASH_OVERFLOW = 3,
+  JDEM_ERR_NONFINITE = 4,
+  JDEM_ERR_OOM = 5,
+  JDEM_ERR_TIMEOUT = 6,
+  JDEM_ERR_UNSUPPORTED = 7,
+  JDEM_ERR_CUDA = 8,
+  JDEM_ERR_NOT_READY = 9
+};
+
+enum { JDEM_DOMAIN_FREE = 0, JDEM_DOMAIN_PERIODIC = 1, JDEM_DOMAIN_REFLECT = 2 };
+enum { JDEM_LIN_NONE = 0, JDEM_LIN_VERLET = 1, JDEM_LIN_EULER = 2 };
+enum { JDEM_ROT_NONE = 0, JDEM_ROT_VERLET_SPIRAL = 1, JDEM_ROT_SPIRAL = 2 };
+
+typedef struct JdemHandle JdemHandle;
+
+/* One independent system (a System pytree: domain, integrators, dt). */
+typedef struct {
+  int64_t n;                   /* particles */
+  int32_t domain;              /* JDEM_DOMAIN_*   (System.domain type) */
+  int32_t linear_integrator;   /* JDEM_LIN_*      (System.linear_integrator) */
+  int32_t rotation_integrator; /* JDEM_ROT_*      (System.rotation_integrator) */
+  float dt;                    /* System.dt */
+  float box_size[3];           /* Domain.box_size */
+  float anchor[3];             /* Domain.anchor */
+  float restitution;           /* ReflectDomain.restitution_coefficient */
+  float gravity[3];            /* ForceManager.gravity */
+  float cell_size;             /* DynamicCellList.cell_size (used by the neighbour list) */
+  int32_t search_range;        /* max(DynamicCellList.neighbor_mask) */
+} JdemSystemDesc;
+
+typedef struct {
+  int32_t dim;                  /* 2 or 3, shared by all systems of a handle */
+  int32_t n_systems;            /* >= 1 */
+  const JdemSystemDesc* systems;
+  float skin;                   /* binning margin; 0 re-sorts every step */
+  int32_t n_materials;          /* MaterialTable size M */
+  const float* young_eff;       /* MaterialTable.young_eff, M*M row-major */
+  int32_t bond_width;           /* W of State.bond_id, 0 when there are no bonds */
+  int32_t interact_same_bond_id;/* System.interact_same_bond_id */
+  int32_t chunk_steps;          /* steps per captured CUDA graph (<= 0: 50) */
+  int32_t device;               /* CUDA device ordinal */
+} JdemConfig;
+
+/* Particle arrays in the reference layout.  Upload reads every field that is
+ * not NULL (rad, mass are required; q/ang_vel/torque/inertia/mat_id/fixed/
+ * bond_id default to identity/zero/State.create defaults when NULL).
+ * Download writes pos_c, vel, force, q, ang_vel, torque when not NULL. */
+typedef struct {
+  float* pos_c;
+  float* vel;
+  float* force;
+  float* q;
+  float* ang_vel;
+  float* torque;
+  float* rad;
+  float* mass;
+  float* inertia;
+  int32_t* mat_id;
+  uint8_t* fixed;
+  int32_t* bond_id;
+} JdemHostState;
+
+typedef struct {
+  int64_t n_particles;
+  int64_t n_cells;
+  int32_t n_systems;
+  int32_t dim;
+  int64_t rebuilds;          /* re-sorts since the last upload */
+  int64_t steps;             /* steps since the last upload */
+  uint32_t device_status;    /* sticky device status bits */
+  int32_t graphs;            /* instantiated CUDA graphs */
+  int64_t device_bytes;      /* device memory held by the handle */
+} JdemStats;
+
+/* ABI version of the loaded library (JDEM_ABI_VERSION). */
+int jdem_abi_version(void);
+/* Human-readable name of a status code. */
+const char* jdem_status_string(int code);
+
+/* System.create: allocate a handle for cfg->n_systems systems.
+ * Replaces the per-slot Create methods (cell_list.py:374-432,
+ * domains/__init__.py:62-121, force_manager.py:80-190) on the device side. */
+int jdem_create(const JdemConfig* cfg, JdemHandle** out);
+int jdem_destroy(JdemHandle* h);
+/* Message of the last failing call on this handle ("" if none). */
+const char* jdem_last_error(const JdemHandle* h);
+
+/* Copy a State (State.create layout, state.py:369-867) to the device.
+ * host: host pointers.  jdem_upload_device takes device pointers. */
+int jdem_upload(JdemHandle* h, const JdemHostState* host);
+int jdem_upload_device(JdemHandle* h, const JdemHostState* dev);
+
+/* System.step(state, system, n) (system.py:701-748): n applications of
+ * _step_once (system.py:60-82), captured in CUDA graphs of chunk_steps
+ * steps.  Blocks until done and reports device status. */
+int jdem_step(JdemHandle* h, int64_t n);
+/* Same, without waiting; jdem_sync() waits and reports status. */
+int jdem_step_async(JdemHandle* h, int64_t n);
+int jdem_sync(JdemHandle* h);
+/* jdem_step with CUDA-event timing: *total_ms = whole call on the stream,
+ * *force_ms = summed duration of the fused force/integrate kernel launches
+ * (each bracketed by its own events; launched without graphs). */
+int jdem_step_timed(JdemHandle* h, int64_t n, double* total_ms, double* force_ms);
+
+/* Read the State back (reference layout). */
+int jdem_download(JdemHandle* h, JdemHostState* host);
+int jdem_download_device(JdemHandle* h, JdemHostState* dev);
+
+/* DynamicCellList.compute_force (cell_list.py:434-464): contact forces at the
+ * current positions (no gravity, no integration); torque = 0 for spheres.
+ * Results are read with jdem_download. */
+int jdem_compute_force(JdemHandle* h);
+
+/* thermal.compute_energy terms summed over all systems (thermal.py:153-177):
+ * out[0] = collider PE (cell_list.py:466-496), out[1] = gravity PE
+ * (force_manager.py:427-479), out[2] = translational KE, out[3] = rotational KE. */
+int jdem_energy(JdemHandle* h, double out[4]);
+/* Same terms per system: out has 4 * n_systems doubles. */
+int jdem_energy_per_system(JdemHandle* h, double* out);
+
+/* Contact pairs (i < j, global indices, sorted lexicographically) with
+ * |r_ij|^2 < (R_i + R_j)^2 -- the pairs whose spring overlap is positive
+ * (utils/contacts.py:21-86 keeps the slots with nonzero force).  Writes at
+ * most cap pairs to pairs[2*cap]; *count receives the total. */
+int jdem_contacts(JdemHandle* h, int32_t* pairs, int64_t cap, int64_t* count);
+
+/* DynamicCellList.create_neighbor_list (cell_list.py:498-595): per particle,
+ * the indices within cutoff in the reference's stencil order, -1 padded;
+ * out is (N, max_neighbors) int32 in caller order (global indices), and
+ * *overflow is set when a row needed more than max_neighbors slots. */
+int jdem_neighbor_list(JdemHandle* h, float cutoff, int32_t max_neighbors, int32_t* out,
+                       int32_t* overflow);
+
+/* Current Domain.box_size / Domain.anchor per system (n_systems * 3 floats
+ * each, unused axes 0).  For the free domain these are the bounding box of
+ * the last step's FreeDomain.apply (domains/free.py:40-63). */
+int jdem_domain_state(JdemHandle* h, float* box, float* anchor);
+
+int jdem_stats(JdemHandle* h, JdemStats* out);
+/* cudaStream_t the handle launches on (as void*). */
+void* jdem_stream(JdemHandle* h);
+
+/* Page-lock caller host memory for asynchronous copies (cudaHostRegister). */
+int jdem_host_register(void* ptr, size_t bytes);
+int jdem_host_unregister(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JDEM_GB300_H */

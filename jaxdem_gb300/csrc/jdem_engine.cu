@@ -1,0 +1,792 @@
+// Host side of the GB300 DEM step engine: device memory, CUDA-graph chunks
+// and the C ABI declared in include/jdem_gb300.h.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/jdem_gb300.h"
+#include "jdem_device.cuh"
+#include "jdem_kernels.h"
+#include "jdem_internal.h"
+
+using namespace jdem;
+
+namespace {
+
+const char* kStatusNames[] = {"ok",          "bad argument", "capacity overflow", "hash overflow",
+                              "non-finite state", "out of device memory", "timeout",
+                              "unsupported configuration", "CUDA error", "not ready"};
+
+}  // namespace
+
+// ------------------------------------------------------------------ helpers
+
+#define JDEM_CUDA_TRY(h, expr)                                                          \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess) {                                                            \
+      return (h)->fail(_e == cudaErrorMemoryAllocation ? JDEM_ERR_OOM : JDEM_ERR_CUDA,   \
+                       std::string(#expr) + ": " + cudaGetErrorString(_e));            \
+    }                                                                                   \
+  } while (0)
+
+int JdemHandle::fail(int code, const std::string& msg) {
+  err = msg;
+  return code;
+}
+
+void JdemHandle::free_all() {
+  for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+  for (void* p : allocs) cudaFree(p);
+  allocs.clear();
+  alloc_bytes.clear();
+  device_bytes = 0;
+  if (h_status) cudaFreeHost(h_status);
+  h_status = nullptr;
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+  for (auto& e : ev_pool) cudaEventDestroy(e);
+  ev_pool.clear();
+}
+
+int JdemHandle::dalloc(void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(JDEM_ERR_OOM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " +
+                                  cudaGetErrorString(e));
+  }
+  allocs.push_back(*p);
+  alloc_bytes[*p] = bytes;
+  device_bytes += (long long)bytes;
+  return JDEM_OK;
+}
+
+void JdemHandle::dfree(void* p) {
+  if (!p) return;
+  auto it = std::find(allocs.begin(), allocs.end(), p);
+  if (it != allocs.end()) allocs.erase(it);
+  auto jt = alloc_bytes.find(p);
+  if (jt != alloc_bytes.end()) {
+    device_bytes -= (long long)jt->second;
+    alloc_bytes.erase(jt);
+  }
+  cudaFree(p);
+}
+
+void JdemHandle::drop_graphs() {
+  for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+}
+
+// Host restatement of the grid choice: binning cell = 2 r_max + skin, grown
+// until the system's cell count fits the budget (any cell at least as large
+// as the contact range gives the same contact set).
+static void choose_grid(SysParams& sp, int dim, float rmax, float skin, long long np,
+                        const float* lo_bb, const float* hi_bb) {
+  float cell = 2.0f * rmax + skin;
+  if (!(cell > 0.0f)) cell = 1.0f;
+  long long budget = std::max(4096LL, 4 * np);
+  for (int it = 0; it < 200; ++it) {
+    long long tot = 1;
+    for (int a = 0; a < dim; ++a) {
+      long long g;
+      if (sp.domain == DOM_PERIODIC) {
+        g = (long long)std::floor(sp.box[a] / cell);
+        if (g < 1) g = 1;
+      } else if (sp.domain == DOM_REFLECT) {
+        g = (long long)std::ceil(sp.box[a] / cell);
+        if (g < 1) g = 1;
+      } else {
+        double ext = (double)hi_bb[a] - (double)lo_bb[a];
+        g = (long long)std::ceil(ext / cell);
+        if (g < 1) g = 1;
+        g += 2;  // headroom: the bounding box grows as particles move
+      }
+      sp.g[a] = (int)std::min<long long>(g, 1 << 30);
+      tot *= g;
+    }
+    if (tot <= budget) break;
+    cell *= 1.1f;
+  }
+  if (dim == 2) sp.g[2] = 1;
+  sp.cell_bin = cell;
+  for (int a = 0; a < 3; ++a) {
+    sp.glo[a] = sp.domain == DOM_FREE ? lo_bb[a] : sp.anchor[a];
+    sp.gcell[a] = cell;
+  }
+  long long ncell = 1;
+  for (int a = 0; a < dim; ++a) ncell *= sp.g[a];
+  sp.ncap = sp.domain == DOM_FREE ? ncell * 2 : ncell;
+}
+
+int JdemHandle::setup(const JdemConfig* cfg) {
+  if (!cfg || (cfg->dim != 2 && cfg->dim != 3) || cfg->n_systems < 1 || !cfg->systems)
+    return fail(JDEM_ERR_BAD_ARG, "config: dim must be 2 or 3 and n_systems >= 1");
+  if ((uint32_t)cfg->n_systems > TAG_SYS_MASK) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "too many systems");
+  if (cfg->n_materials < 1 || (uint32_t)cfg->n_materials > TAG_MAT_MASK || !cfg->young_eff)
+    return fail(JDEM_ERR_BAD_ARG, "config: n_materials in [1, 2047] and young_eff required");
+  if (cfg->bond_width < 0) return fail(JDEM_ERR_BAD_ARG, "config: bond_width < 0");
+  if (!(cfg->skin >= 0.0f)) return fail(JDEM_ERR_BAD_ARG, "config: skin must be >= 0");
+  dev = cfg->device;
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  dim = cfg->dim;
+  S = cfg->n_systems;
+  skin = cfg->skin;
+  chunk = cfg->chunk_steps > 0 ? cfg->chunk_steps : 50;
+  n_mat = cfg->n_materials;
+  bond_w = cfg->bond_width;
+  interact_same_bond = cfg->interact_same_bond_id;
+  desc.assign(cfg->systems, cfg->systems + S);
+  P = 0;
+  for (int s = 0; s < S; ++s) {
+    const JdemSystemDesc& d = desc[s];
+    if (d.n < 0) return fail(JDEM_ERR_BAD_ARG, "system n < 0");
+    if (d.domain < 0 || d.domain > 2) return fail(JDEM_ERR_BAD_ARG, "unknown domain");
+    if (d.linear_integrator < 0 || d.linear_integrator > 2) return fail(JDEM_ERR_BAD_ARG, "unknown linear integrator");
+    if (d.rotation_integrator < 0 || d.rotation_integrator > 2)
+      return fail(JDEM_ERR_BAD_ARG, "unknown rotation integrator");
+    if (!(d.dt > 0.0f) && !(d.dt == 0.0f)) return fail(JDEM_ERR_BAD_ARG, "dt must be finite");
+    for (int a = 0; a < dim; ++a)
+      if (d.domain != DOM_FREE && !(d.box_size[a] > 0.0f))
+        return fail(JDEM_ERR_BAD_ARG, "box_size must be positive");
+    if (d.domain == DOM_REFLECT && !(d.restitution > 0.0f && d.restitution <= 1.0f))
+      return fail(JDEM_ERR_BAD_ARG, "restitution_coefficient must be in (0, 1]");
+    P += d.n;
+  }
+  if (P >= (1LL << 31) - 1) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "more than 2^31-2 particles");
+  JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  own_stream = true;
+  JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, 64));
+  int rc;
+  size_t p4 = sizeof(float4) * (size_t)std::max(P, 1LL);
+  size_t p1 = sizeof(int32_t) * (size_t)std::max(P, 1LL);
+  for (int k = 0; k < 2; ++k) {
+    if ((rc = dalloc((void**)&b.pos[k], p4))) return rc;
+    if ((rc = dalloc((void**)&b.vel[k], p4))) return rc;
+    if ((rc = dalloc((void**)&b.frc[k], p4))) return rc;
+    if ((rc = dalloc((void**)&b.tag[k], p1))) return rc;
+    if ((rc = dalloc((void**)&b.orig[k], p1))) return rc;
+    if ((rc = dalloc((void**)&b.key[k], p1))) return rc;
+  }
+  if ((rc = dalloc((void**)&b.key_tmp, p1))) return rc;
+  if ((rc = dalloc((void**)&b.slot_tmp, p1))) return rc;
+  if ((rc = dalloc((void**)&b.perm_tmp, p1))) return rc;
+  if ((rc = dalloc((void**)&b.sys, sizeof(SysParams) * S))) return rc;
+  if ((rc = dalloc((void**)&b.ctl, sizeof(Ctl)))) return rc;
+  if ((rc = dalloc((void**)&b.bbox, sizeof(float) * 6 * S))) return rc;
+  if ((rc = dalloc((void**)&d_young, sizeof(float) * n_mat * n_mat))) return rc;
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_young, cfg->young_eff, sizeof(float) * n_mat * n_mat,
+                                      cudaMemcpyHostToDevice, stream));
+  if (bond_w > 0) {
+    if ((rc = dalloc((void**)&d_bond, sizeof(int32_t) * (size_t)std::max(P, 1LL) * bond_w))) return rc;
+  }
+  size_t pd = sizeof(float) * (size_t)std::max(P, 1LL) * dim;
+  int ad = dim == 3 ? 3 : 1;
+  size_t pa = sizeof(float) * (size_t)std::max(P, 1LL) * ad;
+  if ((rc = dalloc((void**)&st_pos, pd))) return rc;
+  if ((rc = dalloc((void**)&st_vel, pd))) return rc;
+  if ((rc = dalloc((void**)&st_frc, pd))) return rc;
+  if ((rc = dalloc((void**)&st_rad, p1))) return rc;
+  if ((rc = dalloc((void**)&st_mass, p1))) return rc;
+  if ((rc = dalloc((void**)&st_mat, p1))) return rc;
+  if ((rc = dalloc((void**)&st_fixed, (size_t)std::max(P, 1LL)))) return rc;
+  if ((rc = dalloc((void**)&st_sys, p1))) return rc;
+  if ((rc = dalloc((void**)&d_q, p4))) return rc;
+  if ((rc = dalloc((void**)&d_w, pa))) return rc;
+  if ((rc = dalloc((void**)&d_tq, pa))) return rc;
+  if ((rc = dalloc((void**)&d_inertia, pa))) return rc;
+  b.young = d_young;
+  b.bond = d_bond;
+  b.P = P;
+  b.S = S;
+  b.n_mat = n_mat;
+  b.bond_w = bond_w;
+  b.interact_same_bond = interact_same_bond;
+  // system index of every particle (caller order)
+  std::vector<int32_t> sys_of((size_t)std::max(P, 1LL));
+  long long off = 0;
+  for (int s = 0; s < S; ++s)
+    for (long long i = 0; i < desc[s].n; ++i) sys_of[(size_t)(off++)] = s;
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_sys, sys_of.data(), sizeof(int32_t) * (size_t)std::max(P, 1LL),
+                                      cudaMemcpyHostToDevice, stream));
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  return JDEM_OK;
+}
+
+// Grid + cell arrays from the uploaded radii (host copy rad_h) and positions.
+int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
+  sys_h.assign((size_t)S, SysParams{});
+  long long c_total = 0, off = 0;
+  any_free = false;
+  for (int s = 0; s < S; ++s) {
+    const JdemSystemDesc& d = desc[s];
+    SysParams& sp = sys_h[s];
+    std::memset(&sp, 0, sizeof(sp));
+    for (int a = 0; a < 3; ++a) {
+      float bx = a < dim ? d.box_size[a] : 1.0f;
+      sp.box[a] = bx;
+      sp.inv_box[a] = 1.0f / bx;  // system.py:69-74
+      sp.anchor[a] = a < dim ? d.anchor[a] : 0.0f;
+      sp.gravity[a] = a < dim ? d.gravity[a] : 0.0f;
+    }
+    sp.domain = d.domain;
+    sp.lin = d.linear_integrator;
+    sp.rot = d.rotation_integrator;
+    sp.dt = d.dt;
+    sp.restitution = d.restitution;
+    sp.p0 = off;
+    sp.np = d.n;
+    float rmax = 0.0f;
+    float lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    if (d.n > 0) {
+      for (int a = 0; a < dim; ++a) {
+        lo[a] = 3.4e38f;
+        hi[a] = -3.4e38f;
+      }
+      for (long long i = off; i < off + d.n; ++i) {
+        float r = rad_h[i];
+        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(JDEM_ERR_BAD_ARG, "radius must be finite and >= 0");
+        rmax = std::max(rmax, r);
+        for (int a = 0; a < dim; ++a) {
+          float x = pos_h[i * dim + a];
+          if (!std::isfinite(x)) return fail(JDEM_ERR_NONFINITE, "non-finite position in upload");
+          lo[a] = std::min(lo[a], x - r);
+          hi[a] = std::max(hi[a], x + r);
+        }
+      }
+    }
+    if (d.domain == DOM_FREE) any_free = true;
+    choose_grid(sp, dim, rmax, skin, d.n, lo, hi);
+    sp.c0 = c_total;
+    c_total += sp.ncap;
+    if (c_total >= (1LL << 31) - 2)
+      return fail(JDEM_ERR_HASH_OVERFLOW, "total cell count exceeds the int32 hash range");
+    off += d.n;
+  }
+  if (c_total != C) {
+    drop_graphs();
+    dfree(b.cell_start);
+    dfree(b.cnt);
+    dfree(b.scan_blk);
+    b.cell_start = b.cnt = b.scan_blk = nullptr;
+    int rc;
+    if ((rc = dalloc((void**)&b.cell_start, sizeof(int32_t) * (size_t)(c_total + 1)))) return rc;
+    if ((rc = dalloc((void**)&b.cnt, sizeof(int32_t) * (size_t)c_total))) return rc;
+    long long nb = (c_total + 2047) / 2048 + 1;
+    if ((rc = dalloc((void**)&b.scan_blk, sizeof(int32_t) * (size_t)nb))) return rc;
+    C = c_total;
+    b.C = C;
+  }
+  JDEM_CUDA_TRY(this, cudaMemsetAsync(b.cnt, 0, sizeof(int32_t) * (size_t)C, stream));
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.sys, sys_h.data(), sizeof(SysParams) * S, cudaMemcpyHostToDevice, stream));
+  return JDEM_OK;
+}
+
+int JdemHandle::reset_ctl() {
+  Ctl c;
+  std::memset(&c, 0, sizeof(c));
+  c.need_rebuild = 1u;
+  c.skin_half = 0.5f * skin;
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, stream));
+  return JDEM_OK;
+}
+
+int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
+  if (!s || !s->pos_c || !s->rad || !s->mass) return fail(JDEM_ERR_BAD_ARG, "upload: pos_c, rad and mass are required");
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  size_t N = (size_t)P;
+  int ad = dim == 3 ? 3 : 1;
+  // host copies of radius and positions for grid planning
+  std::vector<float> rad_h(N), pos_h(N * dim);
+  if (N) {
+    if (device_ptrs) {
+      JDEM_CUDA_TRY(this, cudaMemcpy(rad_h.data(), s->rad, N * 4, cudaMemcpyDeviceToHost));
+      JDEM_CUDA_TRY(this, cudaMemcpy(pos_h.data(), s->pos_c, N * dim * 4, cudaMemcpyDeviceToHost));
+    } else {
+      std::memcpy(rad_h.data(), s->rad, N * 4);
+      std::memcpy(pos_h.data(), s->pos_c, N * dim * 4);
+    }
+  }
+  int rc = plan_cells(rad_h.data(), pos_h.data());
+  if (rc) return rc;
+  if (N && s->mat_id) {
+    // material ids index young_eff on the device: validate them here
+    std::vector<int32_t> mat_h(N);
+    if (device_ptrs) JDEM_CUDA_TRY(this, cudaMemcpy(mat_h.data(), s->mat_id, N * 4, cudaMemcpyDeviceToHost));
+    else std::memcpy(mat_h.data(), s->mat_id, N * 4);
+    for (size_t i = 0; i < N; ++i)
+      if (mat_h[i] < 0 || mat_h[i] >= n_mat) return fail(JDEM_ERR_BAD_ARG, "mat_id outside [0, n_materials)");
+  }
+  if (N) {
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_pos, s->pos_c, N * dim * 4, kind, stream));
+    if (s->vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_vel, s->vel, N * dim * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_vel, 0, N * dim * 4, stream));
+    if (s->force) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_frc, s->force, N * dim * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_frc, 0, N * dim * 4, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_rad, s->rad, N * 4, kind, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_mass, s->mass, N * 4, kind, stream));
+    if (s->mat_id) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_mat, s->mat_id, N * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_mat, 0, N * 4, stream));
+    if (s->fixed) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_fixed, s->fixed, N, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_fixed, 0, N, stream));
+    if (bond_w > 0) {
+      if (!s->bond_id) return fail(JDEM_ERR_BAD_ARG, "upload: bond_id required when bond_width > 0");
+      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_bond, s->bond_id, N * bond_w * 4, kind, stream));
+    }
+    // rotational state in caller order
+    std::vector<float> q_h, w_h, t_h, i_h;
+    bool rot_nonzero = false;
+    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, s->q, N * 16, kind, stream));
+    else {
+      q_h.assign(N * 4, 0.0f);
+      for (size_t i = 0; i < N; ++i) q_h[i * 4] = 1.0f;
+      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, q_h.data(), N * 16, cudaMemcpyHostToDevice, stream));
+      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    }
+    if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_w, s->ang_vel, N * ad * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
+    if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tq, s->torque, N * ad * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
+    if (s->inertia) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, s->inertia, N * ad * 4, kind, stream));
+    else {
+      // State.create default: 0.4 m r^2 (3D) / 0.5 m r^2 (2D), state.py:817-823
+      std::vector<float> mass_h(N);
+      if (device_ptrs) JDEM_CUDA_TRY(this, cudaMemcpy(mass_h.data(), s->mass, N * 4, cudaMemcpyDeviceToHost));
+      else std::memcpy(mass_h.data(), s->mass, N * 4);
+      i_h.assign(N * ad, 0.0f);
+      float coeff = dim == 2 ? 0.5f : 0.4f;
+      for (size_t i = 0; i < N; ++i)
+        for (int a = 0; a < ad; ++a) i_h[i * ad + a] = coeff * mass_h[i] * rad_h[i] * rad_h[i];
+      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, i_h.data(), N * ad * 4, cudaMemcpyHostToDevice, stream));
+      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    }
+    // Is any rotational update non-trivial?  With omega = torque = 0 and
+    // q = identity every rotation integrator and the reflect renormalisation
+    // leave the state bit-identical, so the rotation kernel can be skipped.
+    {
+      std::vector<float> qq(N * 4), ww(N * ad), tt(N * ad);
+      if (device_ptrs || !s->q) JDEM_CUDA_TRY(this, cudaMemcpy(qq.data(), d_q, N * 16, cudaMemcpyDeviceToHost));
+      else std::memcpy(qq.data(), s->q, N * 16);
+      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+      JDEM_CUDA_TRY(this, cudaMemcpy(ww.data(), d_w, N * ad * 4, cudaMemcpyDeviceToHost));
+      JDEM_CUDA_TRY(this, cudaMemcpy(tt.data(), d_tq, N * ad * 4, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < N && !rot_nonzero; ++i) {
+        if (qq[i * 4] != 1.0f || qq[i * 4 + 1] != 0.0f || qq[i * 4 + 2] != 0.0f || qq[i * 4 + 3] != 0.0f)
+          rot_nonzero = true;
+        for (int a = 0; a < ad; ++a)
+          if (ww[i * ad + a] != 0.0f || tt[i * ad + a] != 0.0f) rot_nonzero = true;
+      }
+    }
+    rot_active = rot_nonzero;
+    launch_pack(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, st_mat, st_fixed, st_sys, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+  }
+  rc = reset_ctl();
+  if (rc) return rc;
+  cur_box.assign((size_t)S * 3, 0.0f);
+  cur_anchor.assign((size_t)S * 3, 0.0f);
+  for (int s2 = 0; s2 < S; ++s2)
+    for (int a = 0; a < 3; ++a) {
+      cur_box[(size_t)s2 * 3 + a] = a < dim ? desc[s2].box_size[a] : 0.0f;
+      cur_anchor[(size_t)s2 * 3 + a] = a < dim ? desc[s2].anchor[a] : 0.0f;
+    }
+  bbox_pending = false;
+  steps_done = 0;
+  sticky_status = 0;
+  uploaded = true;
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  return JDEM_OK;
+}
+
+// One step's device work after the first drift: re-sort if needed, then the
+// fused force kernel.
+void JdemHandle::enqueue_step(int mode) {
+  launch_rebuild(dim, b, any_free, stream);
+  launch_force(dim, b, mode, stream);
+}
+
+int JdemHandle::run_graph(long long nsteps, int mode_last) {
+  // key: (nsteps, mode of the final step)
+  long long key = nsteps * 64 + mode_last;
+  auto it = graphs.find(key);
+  if (it == graphs.end()) {
+    cudaGraph_t g;
+    JDEM_CUDA_TRY(this, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (long long k = 0; k < nsteps; ++k) enqueue_step(k + 1 == nsteps ? mode_last : MODE_STEP);
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) return fail(JDEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(JDEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    it = graphs.emplace(key, ge).first;
+  }
+  JDEM_CUDA_TRY(this, cudaGraphLaunch(it->second, stream));
+  return JDEM_OK;
+}
+
+int JdemHandle::step_async(long long n) {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "step before upload");
+  if (n < 0) return fail(JDEM_ERR_BAD_ARG, "n < 0");
+  if (n == 0 || P == 0) {
+    steps_done += n;
+    return JDEM_OK;
+  }
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  int bbox = any_free ? MODE_BBOX : 0;
+  if (any_free) {
+    // ordered-int encodings of +inf (min slots) and -inf (max slots)
+    std::vector<unsigned int> init((size_t)S * 6);
+    for (int s = 0; s < S; ++s)
+      for (int a = 0; a < 3; ++a) {
+        init[s * 6 + a] = 0xFFFFFFFFu;
+        init[s * 6 + 3 + a] = 0u;
+      }
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.bbox, init.data(), sizeof(unsigned int) * S * 6,
+                                        cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  }
+  launch_pre(dim, b, n == 1 ? bbox : 0, stream);
+  JDEM_CUDA_TRY(this, cudaGetLastError());
+  // steps 1 .. n-1 run MODE_STEP (their epilogue starts the next step);
+  // step n-1 also records the free-domain box; step n is MODE_STEP_LAST.
+  long long mid = n - 1;
+  long long plain = any_free && mid > 0 ? mid - 1 : mid;
+  int rc;
+  while (plain >= chunk) {
+    if ((rc = run_graph(chunk, MODE_STEP))) return rc;
+    plain -= chunk;
+  }
+  if (plain > 0)
+    if ((rc = run_graph(plain, MODE_STEP))) return rc;
+  if (any_free && mid > 0)
+    if ((rc = run_graph(1, MODE_STEP | MODE_BBOX))) return rc;
+  if ((rc = run_graph(1, MODE_STEP_LAST))) return rc;
+  if (rot_active) {
+    launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+  }
+  if (any_free) bbox_pending = true;
+  steps_done += n;
+  return JDEM_OK;
+}
+
+int JdemHandle::sync_status() {
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(h_status, b.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  const Ctl* c = (const Ctl*)h_status;
+  sticky_status |= c->status;
+  rebuilds = c->rebuilds;
+  if (bbox_pending) {
+    // FreeDomain.apply of the last step: box = max - min, anchor = min (free.py:59-63)
+    std::vector<unsigned int> bb((size_t)S * 6);
+    JDEM_CUDA_TRY(this, cudaMemcpy(bb.data(), b.bbox, sizeof(unsigned int) * S * 6, cudaMemcpyDeviceToHost));
+    auto dec = [](unsigned int u) {
+      unsigned int v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+      float f;
+      std::memcpy(&f, &v, 4);
+      return f;
+    };
+    for (int s2 = 0; s2 < S; ++s2) {
+      if (desc[s2].domain != DOM_FREE || desc[s2].n == 0) continue;
+      for (int a = 0; a < dim; ++a) {
+        float lo = dec(bb[(size_t)s2 * 6 + a]), hi = dec(bb[(size_t)s2 * 6 + 3 + a]);
+        cur_box[(size_t)s2 * 3 + a] = hi - lo;
+        cur_anchor[(size_t)s2 * 3 + a] = lo;
+      }
+    }
+    bbox_pending = false;
+  }
+  if (c->status & ST_NONFINITE) return fail(JDEM_ERR_NONFINITE, "non-finite position or velocity");
+  return JDEM_OK;
+}
+
+int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "step before upload");
+  if (n <= 0) return fail(JDEM_ERR_BAD_ARG, "n must be positive");
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  size_t need = (size_t)(2 * n + 2);
+  while (ev_pool.size() < need) {
+    cudaEvent_t e;
+    JDEM_CUDA_TRY(this, cudaEventCreate(&e));
+    ev_pool.push_back(e);
+  }
+  if (any_free) {
+    int rc = step_async(n);  // free domain keeps the graph path (box bookkeeping)
+    if (rc) return rc;
+    return sync_status();
+  }
+  JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[0], stream));
+  launch_pre(dim, b, 0, stream);
+  for (long long k = 0; k < n; ++k) {
+    launch_rebuild(dim, b, any_free, stream);
+    JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[2 + 2 * k], stream));
+    launch_force(dim, b, k + 1 == n ? MODE_STEP_LAST : MODE_STEP, stream);
+    JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[3 + 2 * k], stream));
+  }
+  if (rot_active) launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
+  JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[1], stream));
+  JDEM_CUDA_TRY(this, cudaGetLastError());
+  JDEM_CUDA_TRY(this, cudaEventSynchronize(ev_pool[1]));
+  float ms = 0.0f;
+  JDEM_CUDA_TRY(this, cudaEventElapsedTime(&ms, ev_pool[0], ev_pool[1]));
+  double fsum = 0.0;
+  for (long long k = 0; k < n; ++k) {
+    float f = 0.0f;
+    JDEM_CUDA_TRY(this, cudaEventElapsedTime(&f, ev_pool[2 + 2 * k], ev_pool[3 + 2 * k]));
+    fsum += f;
+  }
+  if (total_ms) *total_ms = ms;
+  if (force_ms) *force_ms = fsum;
+  steps_done += n;
+  return sync_status();
+}
+
+int JdemHandle::download(JdemHostState* s, bool device_ptrs) {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "download before upload");
+  if (!s) return fail(JDEM_ERR_BAD_ARG, "download: null state");
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  size_t N = (size_t)P;
+  int ad = dim == 3 ? 3 : 1;
+  if (N) {
+    launch_unpack(dim, b, st_pos, st_vel, st_frc, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+    if (s->pos_c) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->pos_c, st_pos, N * dim * 4, kind, stream));
+    if (s->vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->vel, st_vel, N * dim * 4, kind, stream));
+    if (s->force) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->force, st_frc, N * dim * 4, kind, stream));
+    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->q, d_q, N * 16, kind, stream));
+    if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->ang_vel, d_w, N * ad * 4, kind, stream));
+    if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->torque, d_tq, N * ad * 4, kind, stream));
+  }
+  return sync_status();
+}
+
+int JdemHandle::compute_force() {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "compute_force before upload");
+  if (P == 0) return JDEM_OK;
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  launch_rebuild(dim, b, any_free, stream);
+  launch_force(dim, b, MODE_FORCE_ONLY, stream);
+  int ad = dim == 3 ? 3 : 1;
+  JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));
+  JDEM_CUDA_TRY(this, cudaGetLastError());
+  return sync_status();
+}
+
+int JdemHandle::energy(double* out, bool per_system) {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "energy before upload");
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  int ns = per_system ? S : 1;
+  std::vector<double> acc((size_t)ns * 4, 0.0);
+  if (P > 0) {
+    // the binning is kept valid for the current positions by the skin
+    // criterion; the rebuild kernels return at once unless a re-sort is due
+    launch_rebuild(dim, b, any_free, stream);
+    double* d_out = nullptr;
+    int rc;
+    if ((rc = dalloc((void**)&d_out, sizeof(double) * 4 * (size_t)P))) return rc;
+    launch_energy(dim, b, d_out, stream);
+    launch_ke_rot(dim, (long long)P, (const float4*)d_q, d_w, d_inertia, d_out + 3 * (size_t)P, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+    std::vector<double> h((size_t)P * 4);
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(h.data(), d_out, sizeof(double) * 4 * (size_t)P, cudaMemcpyDeviceToHost, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    dfree(d_out);
+    long long off = 0;
+    for (int s = 0; s < S; ++s) {
+      int o = per_system ? s : 0;
+      for (long long i = off; i < off + desc[s].n; ++i) {
+        for (int c = 0; c < 3; ++c) acc[(size_t)o * 4 + c] += h[(size_t)i * 3 + c];
+        acc[(size_t)o * 4 + 3] += h[3 * (size_t)P + (size_t)i];
+      }
+      off += desc[s].n;
+    }
+  }
+  for (size_t k = 0; k < acc.size(); ++k) out[k] = acc[k];
+  return sync_status();
+}
+
+int JdemHandle::contacts(int32_t* pairs, long long cap, long long* count) {
+  if (!uploaded) return fail(JDEM_ERR_NOT_READY, "contacts before upload");
+  if (!count || (cap > 0 && !pairs)) return fail(JDEM_ERR_BAD_ARG, "contacts: null output");
+  *count = 0;
+  if (P == 0) return JDEM_OK;
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  launch_rebuild(dim, b, any_free, stream);
+  int32_t* d_cnt = nullptr;
+  long long* d_off = nullptr;
+  int rc;
+  if ((rc = dalloc((void**)&d_cnt, sizeof(int32_t) * (size_t)P))) return rc;
+  launch_contacts(dim, b, 0, d_cnt, nullptr, nullptr, 0, stream);
+  std::vector<int32_t> cnt((size_t)P);
+  JDEM_CUDA_TRY(this, cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int32_t) * (size_t)P, cudaMemcpyDeviceToHost, stream));
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  std::vector<long long> off((size_t)P);
+  long long tot = 0;
+  for (long long t = 0; t < P; ++t) {
+    off[(size_t)t] = tot;
+    tot += cnt[(size_t)t];
+  }
+  *count = tot;
+  if (tot > 0) {
+    int32_t* d_pairs = nullptr;
+    if ((rc = dalloc((void**)&d_off, sizeof(long long) * (size_t)P))) return rc;
+    if ((rc = dalloc((void**)&d_pairs, sizeof(int32_t) * 2 * (size_t)tot))) return rc;
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_off, off.data(), sizeof(long long) * (size_t)P, cudaMemcpyHostToDevice, stream));
+    launch_contacts(dim, b, 1, nullptr, d_off, d_pairs, tot, stream);
+    std::vector<int32_t> hp((size_t)tot * 2);
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(hp.data(), d_pairs, sizeof(int32_t) * 2 * (size_t)tot, cudaMemcpyDeviceToHost, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    dfree(d_pairs);
+    dfree(d_off);
+    std::vector<long long> keys((size_t)tot);
+    for (long long k = 0; k < tot; ++k) keys[(size_t)k] = ((long long)hp[2 * k] << 32) | (uint32_t)hp[2 * k + 1];
+    std::sort(keys.begin(), keys.end());
+    long long w = std::min(cap, tot);
+    for (long long k = 0; k < w; ++k) {
+      pairs[2 * k] = (int32_t)(keys[(size_t)k] >> 32);
+      pairs[2 * k + 1] = (int32_t)(keys[(size_t)k] & 0xFFFFFFFFLL);
+    }
+  }
+  dfree(d_cnt);
+  return sync_status();
+}
+
+// ------------------------------------------------------------------- C ABI
+
+extern "C" {
+
+int jdem_abi_version(void) { return JDEM_ABI_VERSION; }
+
+const char* jdem_status_string(int code) {
+  if (code < 0 || code > 9) return "unknown status";
+  return kStatusNames[code];
+}
+
+int jdem_create(const JdemConfig* cfg, JdemHandle** out) {
+  if (!out) return JDEM_ERR_BAD_ARG;
+  *out = nullptr;
+  JdemHandle* h = new (std::nothrow) JdemHandle();
+  if (!h) return JDEM_ERR_OOM;
+  int rc = h->setup(cfg);
+  if (rc) {
+    std::fprintf(stderr, "jdem_create: %s\n", h->err.c_str());
+    h->free_all();
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return JDEM_OK;
+}
+
+int jdem_destroy(JdemHandle* h) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  h->free_all();
+  delete h;
+  return JDEM_OK;
+}
+
+const char* jdem_last_error(const JdemHandle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int jdem_upload(JdemHandle* h, const JdemHostState* s) { return h ? h->upload(s, false) : JDEM_ERR_BAD_ARG; }
+int jdem_upload_device(JdemHandle* h, const JdemHostState* s) { return h ? h->upload(s, true) : JDEM_ERR_BAD_ARG; }
+
+int jdem_step(JdemHandle* h, int64_t n) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  int rc = h->step_async(n);
+  if (rc) return rc;
+  return h->sync_status();
+}
+
+int jdem_step_async(JdemHandle* h, int64_t n) { return h ? h->step_async(n) : JDEM_ERR_BAD_ARG; }
+int jdem_sync(JdemHandle* h) { return h ? h->sync_status() : JDEM_ERR_BAD_ARG; }
+
+int jdem_step_timed(JdemHandle* h, int64_t n, double* total_ms, double* force_ms) {
+  return h ? h->step_timed(n, total_ms, force_ms) : JDEM_ERR_BAD_ARG;
+}
+
+int jdem_download(JdemHandle* h, JdemHostState* s) { return h ? h->download(s, false) : JDEM_ERR_BAD_ARG; }
+int jdem_download_device(JdemHandle* h, JdemHostState* s) { return h ? h->download(s, true) : JDEM_ERR_BAD_ARG; }
+int jdem_compute_force(JdemHandle* h) { return h ? h->compute_force() : JDEM_ERR_BAD_ARG; }
+
+int jdem_energy(JdemHandle* h, double out[4]) {
+  if (!h || !out) return JDEM_ERR_BAD_ARG;
+  return h->energy(out, false);
+}
+
+int jdem_energy_per_system(JdemHandle* h, double* out) {
+  if (!h || !out) return JDEM_ERR_BAD_ARG;
+  return h->energy(out, true);
+}
+
+int jdem_contacts(JdemHandle* h, int32_t* pairs, int64_t cap, int64_t* count) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  long long c = 0;
+  int rc = h->contacts(pairs, cap, &c);
+  if (count) *count = c;
+  return rc;
+}
+
+int jdem_neighbor_list(JdemHandle* h, float cutoff, int32_t max_neighbors, int32_t* out, int32_t* overflow) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  return h->neighbor_list(cutoff, max_neighbors, out, overflow);
+}
+
+int jdem_domain_state(JdemHandle* h, float* box, float* anchor) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  return h->domain_state(box, anchor);
+}
+
+int jdem_stats(JdemHandle* h, JdemStats* out) {
+  if (!h || !out) return JDEM_ERR_BAD_ARG;
+  if (h->uploaded) {
+    int rc = h->sync_status();
+    if (rc && rc != JDEM_ERR_NONFINITE) return rc;
+  }
+  out->n_particles = h->P;
+  out->n_cells = h->C;
+  out->n_systems = h->S;
+  out->dim = h->dim;
+  out->rebuilds = h->rebuilds;
+  out->steps = h->steps_done;
+  out->device_status = h->sticky_status;
+  out->graphs = (int32_t)h->graphs.size();
+  out->device_bytes = h->device_bytes;
+  return JDEM_OK;
+}
+
+void* jdem_stream(JdemHandle* h) { return h ? (void*)h->stream : nullptr; }
+
+int jdem_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return JDEM_ERR_BAD_ARG;
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return JDEM_ERR_CUDA;
+  }
+  return JDEM_OK;
+}
+
+int jdem_host_unregister(void* ptr) {
+  if (!ptr) return JDEM_ERR_BAD_ARG;
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return JDEM_ERR_CUDA;
+  }
+  return JDEM_OK;
+}
+
+}  // extern "C"

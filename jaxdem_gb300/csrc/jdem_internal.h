@@ -1,0 +1,75 @@
+// Host-side handle of the GB300 DEM step engine (not part of the public ABI).
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/jdem_gb300.h"
+#include "jdem_device.cuh"
+
+struct JdemHandle {
+  // configuration
+  int dev = 0;
+  int dim = 3;
+  int S = 0;
+  long long P = 0;
+  long long C = 0;
+  float skin = 0.0f;
+  int chunk = 50;
+  int n_mat = 1;
+  int bond_w = 0;
+  int interact_same_bond = 0;
+  std::vector<JdemSystemDesc> desc;
+  std::vector<jdem::SysParams> sys_h;
+  bool any_free = false;
+  bool rot_active = false;
+  bool uploaded = false;
+  bool bbox_pending = false;
+  // current domain frame per system (free domain: last apply's bounding box)
+  std::vector<float> cur_box, cur_anchor;
+
+  // device state
+  jdem::Bufs b{};
+  float* d_young = nullptr;
+  int32_t* d_bond = nullptr;
+  float *st_pos = nullptr, *st_vel = nullptr, *st_frc = nullptr, *st_rad = nullptr, *st_mass = nullptr;
+  int32_t *st_mat = nullptr, *st_sys = nullptr;
+  uint8_t* st_fixed = nullptr;
+  float4* d_q4 = nullptr;
+  float *d_q = nullptr, *d_w = nullptr, *d_tq = nullptr, *d_inertia = nullptr;
+
+  // runtime
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  void* h_status = nullptr;
+  std::map<long long, cudaGraphExec_t> graphs;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<void*> allocs;
+  std::map<void*, size_t> alloc_bytes;
+  long long device_bytes = 0;
+  long long steps_done = 0;
+  long long rebuilds = 0;
+  unsigned int sticky_status = 0;
+  std::string err;
+
+  int fail(int code, const std::string& msg);
+  void free_all();
+  int dalloc(void** p, size_t bytes);
+  void dfree(void* p);
+  void drop_graphs();
+  int setup(const JdemConfig* cfg);
+  int plan_cells(const float* rad_h, const float* pos_h);
+  int reset_ctl();
+  int upload(const JdemHostState* s, bool device_ptrs);
+  void enqueue_step(int mode);
+  int run_graph(long long nsteps, int mode_last);
+  int step_async(long long n);
+  int sync_status();
+  int step_timed(long long n, double* total_ms, double* force_ms);
+  int download(JdemHostState* s, bool device_ptrs);
+  int compute_force();
+  int energy(double* out, bool per_system);
+  int contacts(int32_t* pairs, long long cap, long long* count);
+  int neighbor_list(float cutoff, int max_neighbors, int32_t* out, int32_t* overflow);
+  int domain_state(float* box, float* anchor);
+};

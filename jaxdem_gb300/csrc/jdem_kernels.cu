@@ -1,0 +1,925 @@
+// Kernels of the GB300 DEM step engine.
+//
+// Per step, in steady state, one kernel runs: k_force<DIM> evaluates the
+// spring contact force of every particle against the particles binned in its
+// 3^DIM stencil, adds gravity, applies the after-force half kick and, in the
+// same pass, the next step's wall reflection, before-force half kick and drift
+// (system.py:60-82 order).  Re-binning (counting sort by cell) runs only when
+// the accumulated displacement bound exceeds half the skin; the rebuild
+// kernels read a device flag and return at once otherwise.
+//
+// No atomics touch forces: every pair is evaluated from both sides, as the
+// reference does (cell_list.py:222-260), and each thread sums its own row with
+// a compensated (two-sum) accumulator, so results are deterministic.
+#include "jdem_device.cuh"
+#include "jdem_kernels.h"
+
+namespace jdem {
+
+// ---------------------------------------------------------------- utilities
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v > w ? v : w;
+  }
+  return v;
+}
+
+// Block max of a non-negative float, then one atomicMax per block; the last
+// block to finish folds the kernel's maximum into the displacement bound and
+// raises need_rebuild.  No thread waits on another.
+__device__ void finish_displacement(Ctl* ctl, float d2, bool flip_pos) {
+  __shared__ float red[32];
+  __shared__ bool is_last;
+  d2 = warp_max(d2);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = d2;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    float v = lane < nw ? red[lane] : 0.0f;
+    v = warp_max(v);
+    if (lane == 0) {
+      if (v > 0.0f) atomicMax(&ctl->maxdisp2, __float_as_uint(v));
+      __threadfence();
+      unsigned int prev = atomicAdd(&ctl->done, 1u);
+      is_last = (prev == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    float m2 = __uint_as_float(atomicExch(&ctl->maxdisp2, 0u));
+    float b = ctl->bound + sqrtf(m2);
+    ctl->bound = b;
+    if (b > ctl->skin_half) ctl->need_rebuild = 1u;
+    if (flip_pos) ctl->pos_sel ^= 1u;
+    ctl->done = 0u;
+  }
+}
+
+// ------------------------------------------------------------ pack / unpack
+
+// Caller-order staging arrays -> slot arrays (identity order); a re-sort
+// follows before the first force evaluation.
+template <int DIM>
+__global__ void k_pack(Bufs b, const float* __restrict__ pos, const float* __restrict__ vel,
+                       const float* __restrict__ frc, const float* __restrict__ rad,
+                       const float* __restrict__ mass, const int32_t* __restrict__ mat,
+                       const uint8_t* __restrict__ fixed, const int32_t* __restrict__ sys_of) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= b.P) return;
+  float p[3] = {0, 0, 0}, v[3] = {0, 0, 0}, f[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    p[a] = pos[i * DIM + a];
+    v[a] = vel[i * DIM + a];
+    f[a] = frc[i * DIM + a];
+  }
+  b.pos[0][i] = make_float4(p[0], p[1], p[2], rad[i]);
+  b.pos[1][i] = b.pos[0][i];
+  b.vel[0][i] = make_float4(v[0], v[1], v[2], mass[i]);
+  b.frc[0][i] = make_float4(f[0], f[1], f[2], 0.0f);
+  uint32_t tg = (uint32_t)sys_of[i] | (((uint32_t)mat[i] & TAG_MAT_MASK) << TAG_MAT_SHIFT) |
+                (fixed[i] ? TAG_FIXED : 0u);
+  b.tag[0][i] = tg;
+  b.orig[0][i] = (int32_t)i;
+  b.key[0][i] = 0;
+}
+
+// Slot arrays -> caller order (reference (N, dim) layout).
+template <int DIM>
+__global__ void k_unpack(Bufs b, float* __restrict__ pos, float* __restrict__ vel,
+                         float* __restrict__ frc) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  long long i = b.orig[sel][t];
+  float4 p = b.pos[ps][t], v = b.vel[sel][t], f = b.frc[sel][t];
+  pos[i * DIM + 0] = p.x;
+  pos[i * DIM + 1] = p.y;
+  vel[i * DIM + 0] = v.x;
+  vel[i * DIM + 1] = v.y;
+  frc[i * DIM + 0] = f.x;
+  frc[i * DIM + 1] = f.y;
+  if (DIM == 3) {
+    pos[i * DIM + 2] = p.z;
+    vel[i * DIM + 2] = v.z;
+    frc[i * DIM + 2] = f.z;
+  }
+}
+
+// --------------------------------------------------------------- re-binning
+
+// Free domain: binning frame = bounding box of the spheres (domains/free.py:59-63),
+// one block per free system; grid capped at the system's cell capacity.
+template <int DIM>
+__global__ void k_grid_free(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  int s = blockIdx.x;
+  SysParams& sp = b.sys[s];
+  if (sp.domain != DOM_FREE) return;
+  unsigned int ps = ld_cg_u32(&b.ctl->pos_sel);
+  float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (long long t = sp.p0 + threadIdx.x; t < sp.p0 + sp.np; t += blockDim.x) {
+    float4 p = b.pos[ps][t];
+    float pa[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      lo[a] = fminf(lo[a], pa[a] - p.w);
+      hi[a] = fmaxf(hi[a], pa[a] + p.w);
+    }
+  }
+  __shared__ float slo[3][256], shi[3][256];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    slo[a][threadIdx.x] = lo[a];
+    shi[a][threadIdx.x] = hi[a];
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int a = 0; a < 3; ++a) {
+        slo[a][threadIdx.x] = fminf(slo[a][threadIdx.x], slo[a][threadIdx.x + w]);
+        shi[a][threadIdx.x] = fmaxf(shi[a][threadIdx.x], shi[a][threadIdx.x + w]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double cell = sp.cell_bin;
+    long long g[3] = {1, 1, 1};
+    for (int it = 0; it < 64; ++it) {
+      long long tot = 1;
+      for (int a = 0; a < DIM; ++a) {
+        double ext = (double)shi[a][0] - (double)slo[a][0];
+        double q = ext / cell;
+        g[a] = (q >= 1.0 && q < 1.0e9) ? (long long)ceil(q) : 1;
+        if (g[a] > sp.ncap) g[a] = sp.ncap;
+        tot *= g[a];
+      }
+      if (tot <= sp.ncap) break;
+      cell *= 1.26;
+    }
+    long long tot = 1;
+    for (int a = 0; a < DIM; ++a) tot *= g[a];
+    if (tot > sp.ncap)
+      for (int a = 0; a < DIM; ++a) g[a] = 1;  // non-finite extent: one cell, still correct
+    for (int a = 0; a < DIM; ++a) {
+      sp.glo[a] = isfinite(slo[a][0]) ? slo[a][0] : 0.0f;
+      sp.gcell[a] = (float)cell;
+      sp.g[a] = (int)g[a];
+    }
+    if (DIM == 2) sp.g[2] = 1;
+  }
+}
+
+// Cell key of every slot + per-cell occupancy (the rank inside the cell comes
+// from the atomic and is made deterministic by k_cellsort).
+template <int DIM>
+__global__ void k_bin(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  float4 p = b.pos[ps][t];
+  uint32_t tg = b.tag[sel][t];
+  const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
+  int cx = cell_coord(sp, 0, p.x);
+  int cy = cell_coord(sp, 1, p.y);
+  long long local = (long long)cy * sp.g[0] + cx;
+  if (DIM == 3) {
+    int cz = cell_coord(sp, 2, p.z);
+    local += (long long)cz * sp.g[0] * sp.g[1];
+  }
+  int key = (int)(sp.c0 + local);
+  b.key_tmp[t] = key;
+  b.slot_tmp[t] = atomicAdd(&b.cnt[key], 1);
+}
+
+constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_TILE = SCAN_T * SCAN_V;
+
+// exclusive scan of cnt[0..C) -> cell_start[0..C], cell_start[C] = P.
+__device__ __forceinline__ int block_excl_scan(int v, int* sh, int& total) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    int w = lane < nw ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) sh[lane] = w;
+  }
+  __syncthreads();
+  int warp_off = wid > 0 ? sh[wid - 1] : 0;
+  total = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+__global__ void k_scan_reduce(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ int sh[32];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; ++k) {
+    long long c = base + (long long)threadIdx.x * SCAN_V + k;
+    if (c < b.C) s += b.cnt[c];
+  }
+  int total;
+  block_excl_scan(s, sh, total);
+  if (threadIdx.x == 0) b.scan_blk[blockIdx.x] = total;
+}
+
+__global__ void k_scan_top(Bufs b, int nblk) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ int sh[32];
+  // one block of 1024 threads, each owning a run of ceil(nblk/1024) entries
+  int per = (nblk + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(nblk, lo + per);
+  int s = 0;
+  for (int i = lo; i < hi; ++i) s += b.scan_blk[i];
+  int total;
+  int off = block_excl_scan(s, sh, total);
+  for (int i = lo; i < hi; ++i) {
+    int v = b.scan_blk[i];
+    b.scan_blk[i] = off;
+    off += v;
+  }
+}
+
+__global__ void k_scan_down(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ int sh[32];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  int v[SCAN_V];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; ++k) {
+    long long c = base + (long long)threadIdx.x * SCAN_V + k;
+    v[k] = c < b.C ? b.cnt[c] : 0;
+    s += v[k];
+  }
+  int total;
+  int off = block_excl_scan(s, sh, total) + b.scan_blk[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < SCAN_V; ++k) {
+    long long c = base + (long long)threadIdx.x * SCAN_V + k;
+    if (c < b.C) b.cell_start[c] = off;
+    off += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) b.cell_start[b.C] = (int)b.P;
+}
+
+__global__ void k_scatter(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  int key = b.key_tmp[t];
+  b.perm_tmp[b.cell_start[key] + b.slot_tmp[t]] = (int)t;
+}
+
+// Per cell: order the cell's slots by original index (the stable order of
+// lax.sort([hash, iota]), cell_list.py:64) and clear the occupancy counter.
+__global__ void k_cellsort(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= b.C) return;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel);
+  int a = b.cell_start[c], e = b.cell_start[c + 1];
+  b.cnt[c] = 0;
+  const int32_t* orig = b.orig[sel];
+  for (int i = a + 1; i < e; ++i) {
+    int x = b.perm_tmp[i];
+    int ox = orig[x];
+    int j = i - 1;
+    while (j >= a && orig[b.perm_tmp[j]] > ox) {
+      b.perm_tmp[j + 1] = b.perm_tmp[j];
+      --j;
+    }
+    b.perm_tmp[j + 1] = x;
+  }
+}
+
+// Gather every slot array into the spare copy in sorted order, then flip.
+__global__ void k_gather(Bufs b) {
+  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ bool is_last;
+  long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  if (u < b.P) {
+    int t = b.perm_tmp[u];
+    b.pos[ps ^ 1u][u] = b.pos[ps][t];
+    b.vel[sel ^ 1u][u] = b.vel[sel][t];
+    b.frc[sel ^ 1u][u] = b.frc[sel][t];
+    b.tag[sel ^ 1u][u] = b.tag[sel][t];
+    b.orig[sel ^ 1u][u] = b.orig[sel][t];
+    b.key[sel ^ 1u][u] = b.key_tmp[t];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned int prev = atomicAdd(&b.ctl->done2, 1u);
+    is_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    b.ctl->sel = sel ^ 1u;
+    b.ctl->pos_sel = ps ^ 1u;
+    b.ctl->need_rebuild = 0u;
+    b.ctl->bound = 0.0f;
+    b.ctl->rebuilds += 1u;
+    b.ctl->done2 = 0u;
+  }
+}
+
+// ------------------------------------------------------------ first drift
+
+// Step 1 of a call: domain.apply (reflect), step_before_force (VV), drift.
+template <int DIM>
+__global__ void k_pre(Bufs b, int mode) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  float d2 = 0.0f;
+  if (t < b.P) {
+    float4 p4 = b.pos[ps][t];
+    float4 v4 = b.vel[sel][t];
+    float4 f4 = b.frc[sel][t];
+    uint32_t tg = b.tag[sel][t];
+    const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
+    bool fixed = (tg & TAG_FIXED) != 0u;
+    float p[3] = {p4.x, p4.y, p4.z}, v[3] = {v4.x, v4.y, v4.z}, F[3] = {f4.x, f4.y, f4.z};
+    float p0[3] = {p[0], p[1], p[2]};
+    float m = v4.w;
+    if ((mode & MODE_BBOX) && sp.domain == DOM_FREE) {
+      int s = tg & TAG_SYS_MASK;
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        atomicMin((unsigned int*)&b.bbox[s * 6 + a], f2ord(p[a] - p4.w));
+        atomicMax((unsigned int*)&b.bbox[s * 6 + 3 + a], f2ord(p[a] + p4.w));
+      }
+    }
+    if (sp.domain == DOM_REFLECT) reflect_sphere<DIM>(sp, p, v, F, p4.w, m, fixed);
+    if (sp.lin == LIN_VERLET) {
+      float sc = sp.dt * 0.5f / m;
+      float fr = fixed ? 0.0f : 1.0f;
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        v[a] = v[a] + F[a] * sc * fr;
+        p[a] = p[a] + sp.dt * v[a];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      float d = p[a] - p0[a];
+      d2 = d2 + d * d;
+    }
+    b.pos[ps][t] = make_float4(p[0], p[1], p[2], p4.w);
+    b.vel[sel][t] = make_float4(v[0], v[1], v[2], m);
+    if (!(d2 == d2) || d2 > 3.0e38f) {
+      atomicOr(&b.ctl->status, ST_NONFINITE);
+      d2 = 0.0f;
+    }
+  }
+  finish_displacement(b.ctl, d2, false);
+}
+
+// ---------------------------------------------------------- fused step
+
+// One thread per slot.  Contact force (spring.py:97-108 with the periodic
+// minimum image of periodic.py:74-79) summed over the stencil, then
+// ForceManager gravity (force_manager.py:393-405), step_after_force, and, in
+// MODE_STEP, the next step's ReflectDomain.apply, step_before_force and drift.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_force(Bufs b, int mode) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  int base_mode = mode & 7;
+  float d2max = 0.0f;
+  if (t < b.P) {
+    const float4* __restrict__ P = b.pos[ps];
+    const int32_t* __restrict__ cs = b.cell_start;
+    float4 pi = P[t];
+    uint32_t tg = b.tag[sel][t];
+    int s = tg & TAG_SYS_MASK;
+    const SysParams& sp = b.sys[s];
+    const bool per = sp.domain == DOM_PERIODIC;
+    const float bx = sp.box[0], by = sp.box[1], bz = sp.box[2];
+    const float ibx = sp.inv_box[0], iby = sp.inv_box[1], ibz = sp.inv_box[2];
+    const int gx = sp.g[0], gy = sp.g[1];
+    long long local = b.key[sel][t] - sp.c0;
+    int cx = (int)(local % gx);
+    long long rem = local / gx;
+    int cy = (int)(rem % gy);
+    int cz = DIM == 3 ? (int)(rem / gy) : 0;
+    int ys[3], zs[3];
+    int ny = axis_set(cy, gy, per, ys);
+    int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
+    if (DIM == 2) zs[0] = 0;
+    int xa0, xb0, xa1, xb1;
+    x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
+    const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+    const float k0 = b.young[mat_i * b.n_mat + mat_i];
+    const bool multi_mat = b.n_mat > 1;
+    const bool bonds = b.bond_w > 0;
+    const int oi = bonds ? b.orig[sel][t] : 0;
+    float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+    for (int iz = 0; iz < nz; ++iz) {
+      for (int iy = 0; iy < ny; ++iy) {
+        long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
+        for (int r = 0; r < 2; ++r) {
+          int ca = r == 0 ? xa0 : xa1, cb = r == 0 ? xb0 : xb1;
+          if (ca >= cb) continue;
+          int ja = cs[row + ca], jb = cs[row + cb];
+          for (int j = ja; j < jb; ++j) {
+            float4 pj = P[j];
+            float dx = pi.x - pj.x;
+            float dy = pi.y - pj.y;
+            float dz = DIM == 3 ? pi.z - pj.z : 0.0f;
+            if (per) {
+              dx = dx - bx * rintf(dx * ibx);
+              dy = dy - by * rintf(dy * iby);
+              if (DIM == 3) dz = dz - bz * rintf(dz * ibz);
+            }
+            float dsq = dx * dx + dy * dy;
+            if (DIM == 3) dsq = dsq + dz * dz;
+            float R = pi.w + pj.w;
+            if (dsq < R * R * 1.000001f && j != (int)t) {
+              float k = k0;
+              if (multi_mat) {
+                int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+                k = b.young[mat_i * b.n_mat + mat_j];
+              }
+              if (bonds && !b.interact_same_bond) {
+                int oj = b.orig[sel][j];
+                bool bonded = false;
+                for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
+                if (bonded) continue;
+              }
+              float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
+              float rr = dsq * inv;
+              float delta = R - rr;
+              delta = delta > 0.0f ? delta : 0.0f;
+              float mag = k * delta * inv;
+              two_sum_acc(fx, ex, mag * dx);
+              two_sum_acc(fy, ey, mag * dy);
+              if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
+            }
+          }
+        }
+      }
+    }
+    float F[3] = {fx + ex, fy + ey, DIM == 3 ? fz + ez : 0.0f};
+    if (base_mode == MODE_FORCE_ONLY) {
+      b.frc[sel][t] = make_float4(F[0], F[1], F[2], 0.0f);
+    } else {
+      float4 v4 = b.vel[sel][t];
+      float m = v4.w;
+      bool fixed = (tg & TAG_FIXED) != 0u;
+      float fr = fixed ? 0.0f : 1.0f;
+      float p[3] = {pi.x, pi.y, pi.z}, v[3] = {v4.x, v4.y, v4.z};
+      // ForceManager.apply: F_contact + F_part(0) + gravity * (mass / count)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) F[a] = (F[a] + 0.0f) + sp.gravity[a] * (m / 1.0f);
+      if (sp.lin == LIN_VERLET) {
+        float sc = sp.dt * 0.5f / m;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) v[a] = v[a] + F[a] * sc * fr;
+      } else if (sp.lin == LIN_EULER) {
+        float sc = sp.dt / m;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+          v[a] = v[a] + F[a] * sc * fr;
+          p[a] = p[a] + sp.dt * v[a];
+        }
+      }
+      b.frc[sel][t] = make_float4(F[0], F[1], F[2], 0.0f);
+      if (base_mode == MODE_STEP) {
+        if ((mode & MODE_BBOX) && sp.domain == DOM_FREE) {
+#pragma unroll
+          for (int a = 0; a < DIM; ++a) {
+            atomicMin((unsigned int*)&b.bbox[s * 6 + a], f2ord(p[a] - pi.w));
+            atomicMax((unsigned int*)&b.bbox[s * 6 + 3 + a], f2ord(p[a] + pi.w));
+          }
+        }
+        if (sp.domain == DOM_REFLECT) reflect_sphere<DIM>(sp, p, v, F, pi.w, m, fixed);
+        if (sp.lin == LIN_VERLET) {
+          float sc = sp.dt * 0.5f / m;
+#pragma unroll
+          for (int a = 0; a < DIM; ++a) {
+            v[a] = v[a] + F[a] * sc * fr;
+            p[a] = p[a] + sp.dt * v[a];
+          }
+        }
+      }
+      float pa[3] = {pi.x, pi.y, pi.z};
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        float d = p[a] - pa[a];
+        d2max = d2max + d * d;
+      }
+      b.pos[ps ^ 1u][t] = make_float4(p[0], p[1], p[2], pi.w);
+      b.vel[sel][t] = make_float4(v[0], v[1], v[2], m);
+      if (!(d2max == d2max) || d2max > 3.0e38f) {
+        atomicOr(&b.ctl->status, ST_NONFINITE);
+        d2max = 0.0f;
+      }
+    }
+  }
+  if (base_mode != MODE_FORCE_ONLY) finish_displacement(b.ctl, d2max, true);
+}
+
+// -------------------------------------------------------------- rotation
+
+// Rotational degrees of freedom of smooth spheres, n steps in registers.
+// Spring contacts exert no torque and gravity acts at the centre, so after
+// the first step's before-force update torque is 0; the reflect domain only
+// renormalises q (reflect.py:291-294 with a zero rotation vector).
+// VelocityVerletSpiral: velocity_verlet_spiral.py:83-116, 156-180.
+// Spiral: spiral.py (step_after_force).  omega_dot: spiral.py:22-40.
+template <int DIM>
+__device__ __forceinline__ void omega_dot3(const float* w, const float* tq, const float* I,
+                                           const float* invI, float* out) {
+  if (DIM == 3) {
+    float cx = w[1] * (I[2] * w[2]) - w[2] * (I[1] * w[1]);
+    float cy = w[2] * (I[0] * w[0]) - w[0] * (I[2] * w[2]);
+    float cz = w[0] * (I[1] * w[1]) - w[1] * (I[0] * w[0]);
+    out[0] = (tq[0] - cx) * invI[0];
+    out[1] = (tq[1] - cy) * invI[1];
+    out[2] = (tq[2] - cz) * invI[2];
+  } else {
+    out[0] = tq[0] * invI[0];
+  }
+}
+
+template <int DIM>
+__device__ void ssprk3(float h, const float* w, const float* tq, const float* I, const float* invI,
+                       float fr, float* wout) {
+  constexpr int AD = DIM == 3 ? 3 : 1;
+  float k1[3], k2[3], k3[3], tmp[3];
+  omega_dot3<DIM>(w, tq, I, invI, k1);
+  for (int a = 0; a < AD; ++a) {
+    k1[a] = h * k1[a];
+    tmp[a] = w[a] + k1[a];
+  }
+  omega_dot3<DIM>(tmp, tq, I, invI, k2);
+  for (int a = 0; a < AD; ++a) {
+    k2[a] = h * k2[a];
+    tmp[a] = w[a] + 0.25f * (k1[a] + k2[a]);
+  }
+  omega_dot3<DIM>(tmp, tq, I, invI, k3);
+  for (int a = 0; a < AD; ++a) {
+    k3[a] = h * k3[a];
+    wout[a] = w[a] + fr * (k1[a] + k2[a] + 4.0f * k3[a]) / 6.0f;
+  }
+}
+
+template <int DIM>
+__global__ void k_rot(Bufs b, const int32_t* __restrict__ sys_of, float4* __restrict__ q,
+                      float* __restrict__ angv, float* __restrict__ torque,
+                      const float* __restrict__ inertia, const uint8_t* __restrict__ fixed,
+                      long long nsteps) {
+  constexpr int AD = DIM == 3 ? 3 : 1;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= b.P) return;
+  const SysParams& sp = b.sys[sys_of[i]];
+  const int rot = sp.rot, domain = sp.domain;
+  const float dt = sp.dt;
+  float4 qq = q[i];
+  float w[3] = {0, 0, 0}, tq[3] = {0, 0, 0}, I[3] = {1, 1, 1}, invI[3] = {1, 1, 1};
+  for (int a = 0; a < AD; ++a) {
+    w[a] = angv[i * AD + a];
+    tq[a] = torque[i * AD + a];
+    I[a] = inertia[i * AD + a];
+    invI[a] = 1.0f / I[a];
+  }
+  float fr = fixed[i] ? 0.0f : 1.0f;
+  for (long long s = 0; s < nsteps; ++s) {
+    if (domain == DOM_REFLECT) qq = q_unit(q_mul(make_float4(1.0f - 0.0f / 8.0f, 0.0f, 0.0f, 0.0f), qq));
+    if (rot == ROT_VVSPIRAL) {
+      float dt_2 = dt / 2.0f;
+      float wb[3], tb[3], wn[3];
+      if (DIM == 3) {
+        q_rotate3(qq, -1.0f, w, wb);
+        q_rotate3(qq, -1.0f, tq, tb);
+      } else {
+        wb[0] = w[0];
+        tb[0] = tq[0];
+      }
+      ssprk3<DIM>(dt_2, wb, tb, I, invI, fr, wn);
+      float rv[3];
+      if (DIM == 3) {
+        for (int a = 0; a < 3; ++a) rv[a] = 2.0f * dt_2 * wn[a];
+      } else {
+        float r = 2.0f * dt_2 * wn[0];
+        rv[0] = 0.0f * r;
+        rv[1] = 0.0f * r;
+        rv[2] = 1.0f * r;
+      }
+      float4 dq = q_small_rotvec(rv[0], rv[1], rv[2]);
+      qq = q_unit(q_mul(qq, dq));
+      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
+      else w[0] = wn[0];
+    }
+    // compute_force + ForceManager: torque = 0 + cross(0, F) + 0
+    for (int a = 0; a < AD; ++a) tq[a] = 0.0f;
+    if (rot == ROT_VVSPIRAL) {
+      float dt_2 = dt / 2.0f;
+      float wb[3], tb[3] = {0, 0, 0}, wn[3];
+      if (DIM == 3) q_rotate3(qq, -1.0f, w, wb);
+      else wb[0] = w[0];
+      ssprk3<DIM>(dt_2, wb, tb, I, invI, fr, wn);
+      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
+      else w[0] = wn[0];
+    } else if (rot == ROT_SPIRAL) {
+      float dt_2 = dt / 2.0f;
+      float wb[3], tb[3] = {0, 0, 0}, wd[3], tmp[3], k1[3], k2[3], k3[3];
+      if (DIM == 3) q_rotate3(qq, -1.0f, w, wb);
+      else wb[0] = w[0];
+      omega_dot3<DIM>(wb, tb, I, invI, wd);
+      float rv1[3], rv2[3];
+      if (DIM == 3) {
+        for (int a = 0; a < 3; ++a) {
+          rv1[a] = 2.0f * dt_2 * wb[a];
+          rv2[a] = 2.0f * dt_2 * dt_2 * wd[a];
+        }
+      } else {
+        float r1 = 2.0f * dt_2 * wb[0], r2 = 2.0f * dt_2 * dt_2 * wd[0];
+        rv1[0] = 0.0f * r1; rv1[1] = 0.0f * r1; rv1[2] = 1.0f * r1;
+        rv2[0] = 0.0f * r2; rv2[1] = 0.0f * r2; rv2[2] = 1.0f * r2;
+      }
+      float4 dq = q_mul(q_small_rotvec(rv1[0], rv1[1], rv1[2]), q_small_rotvec(rv2[0], rv2[1], rv2[2]));
+      qq = q_unit(q_mul(qq, dq));
+      for (int a = 0; a < AD; ++a) {
+        k1[a] = dt * wd[a];
+        tmp[a] = wb[a] + k1[a];
+      }
+      omega_dot3<DIM>(tmp, tb, I, invI, k2);
+      for (int a = 0; a < AD; ++a) {
+        k2[a] = dt * k2[a];
+        tmp[a] = wb[a] + 0.25f * (k1[a] + k2[a]);
+      }
+      omega_dot3<DIM>(tmp, tb, I, invI, k3);
+      float wn[3];
+      for (int a = 0; a < AD; ++a) {
+        k3[a] = dt * k3[a];
+        wn[a] = wb[a] + fr * (k1[a] + k2[a] + 4.0f * k3[a]) / 6.0f;
+      }
+      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
+      else w[0] = wn[0];
+    }
+  }
+  q[i] = qq;
+  for (int a = 0; a < AD; ++a) {
+    angv[i * AD + a] = w[a];
+    torque[i * AD + a] = tq[a];
+  }
+}
+
+// ----------------------------------------------------------- diagnostics
+
+// Per-particle energies in caller order: 0.5 * sum_j 0.5 k delta^2
+// (spring.py:110-147, _partition.py:39-51), gravity -m g.x
+// (force_manager.py:450-459) and translational kinetic energy
+// (thermal.py:24-47), as doubles; the host sums them in index order.
+template <int DIM>
+__global__ void k_energy(Bufs b, double* __restrict__ out) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  double e_pair = 0.0, e_grav = 0.0, e_kin = 0.0;
+  const float4* __restrict__ P = b.pos[ps];
+  float4 pi = P[t];
+  uint32_t tg = b.tag[sel][t];
+  const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
+  const bool per = sp.domain == DOM_PERIODIC;
+  const int gx = sp.g[0], gy = sp.g[1];
+  long long local = b.key[sel][t] - sp.c0;
+  int cx = (int)(local % gx);
+  long long rem = local / gx;
+  int cy = (int)(rem % gy);
+  int cz = DIM == 3 ? (int)(rem / gy) : 0;
+  int ys[3], zs[3];
+  int ny = axis_set(cy, gy, per, ys);
+  int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
+  if (DIM == 2) zs[0] = 0;
+  int xa0, xb0, xa1, xb1;
+  x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
+  const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+  const int oi = b.orig[sel][t];
+  for (int iz = 0; iz < nz; ++iz)
+    for (int iy = 0; iy < ny; ++iy) {
+      long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
+      for (int r = 0; r < 2; ++r) {
+        int ca = r == 0 ? xa0 : xa1, cb = r == 0 ? xb0 : xb1;
+        if (ca >= cb) continue;
+        for (int j = b.cell_start[row + ca]; j < b.cell_start[row + cb]; ++j) {
+          if (j == (int)t) continue;
+          float4 pj = P[j];
+          float d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+          if (per)
+            for (int a = 0; a < DIM; ++a) d[a] = d[a] - sp.box[a] * rintf(d[a] * sp.inv_box[a]);
+          float dsq = d[0] * d[0] + d[1] * d[1];
+          if (DIM == 3) dsq = dsq + d[2] * d[2];
+          float R = pi.w + pj.w;
+          if (!(dsq < R * R * 1.000001f)) continue;
+          if (b.bond_w > 0 && !b.interact_same_bond) {
+            int oj = b.orig[sel][j];
+            bool bonded = false;
+            for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
+            if (bonded) continue;
+          }
+          int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+          float k = b.young[mat_i * b.n_mat + mat_j];
+          float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
+          float rr = dsq * inv;
+          float s = R - rr;
+          s = s > 0.0f ? s : 0.0f;
+          float e = 0.5f * k * (s * s);
+          e_pair += (double)(0.5f * e);
+        }
+      }
+    }
+  float4 v4 = b.vel[sel][t];
+  float p[3] = {pi.x, pi.y, pi.z}, v[3] = {v4.x, v4.y, v4.z};
+  for (int a = 0; a < DIM; ++a) {
+    e_grav -= (double)sp.gravity[a] * (double)p[a] * (double)v4.w;
+    e_kin += 0.5 * (double)v4.w * (double)v[a] * (double)v[a];
+  }
+  out[(long long)oi * 3 + 0] = e_pair;
+  out[(long long)oi * 3 + 1] = e_grav;
+  out[(long long)oi * 3 + 2] = e_kin;
+}
+
+// Rotational kinetic energy 0.5 w_b . (I w_b), w_b in the body frame
+// (thermal.py:50-80), caller order.
+template <int DIM>
+__global__ void k_ke_rot(long long N, const float4* __restrict__ q, const float* __restrict__ angv,
+                         const float* __restrict__ inertia, double* __restrict__ out) {
+  constexpr int AD = DIM == 3 ? 3 : 1;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float w[3] = {0, 0, 0}, wb[3] = {0, 0, 0};
+  for (int a = 0; a < AD; ++a) w[a] = angv[i * AD + a];
+  if (DIM == 3) q_rotate3(q[i], -1.0f, w, wb);
+  else wb[0] = w[0];
+  double e = 0.0;
+  for (int a = 0; a < AD; ++a) e += (double)wb[a] * (double)inertia[i * AD + a] * (double)wb[a];
+  out[i] = 0.5 * e;
+}
+
+// Canonical contacts: pairs with orig_i < orig_j and dsq < (ri + rj)^2,
+// evaluated with the same IEEE operations as the oracle.  Pass 0 counts per
+// slot, pass 1 writes (orig_i, orig_j) at the scanned offsets.
+template <int DIM>
+__global__ void k_contacts(Bufs b, int pass, int32_t* __restrict__ counts,
+                           const long long* __restrict__ offs, int32_t* __restrict__ pairs,
+                           long long cap) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  const float4* __restrict__ P = b.pos[ps];
+  float4 pi = P[t];
+  uint32_t tg = b.tag[sel][t];
+  const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
+  const bool per = sp.domain == DOM_PERIODIC;
+  const int gx = sp.g[0], gy = sp.g[1];
+  long long local = b.key[sel][t] - sp.c0;
+  int cx = (int)(local % gx);
+  long long rem = local / gx;
+  int cy = (int)(rem % gy);
+  int cz = DIM == 3 ? (int)(rem / gy) : 0;
+  int ys[3], zs[3];
+  int ny = axis_set(cy, gy, per, ys);
+  int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
+  if (DIM == 2) zs[0] = 0;
+  int xa0, xb0, xa1, xb1;
+  x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
+  int oi = b.orig[sel][t];
+  long long o = pass == 1 ? offs[t] : 0;
+  int c = 0;
+  for (int iz = 0; iz < nz; ++iz)
+    for (int iy = 0; iy < ny; ++iy) {
+      long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
+      for (int r = 0; r < 2; ++r) {
+        int ca = r == 0 ? xa0 : xa1, cb = r == 0 ? xb0 : xb1;
+        if (ca >= cb) continue;
+        for (int j = b.cell_start[row + ca]; j < b.cell_start[row + cb]; ++j) {
+          int oj = b.orig[sel][j];
+          if (oj <= oi) continue;
+          float4 pj = P[j];
+          float d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+          if (per)
+            for (int a = 0; a < DIM; ++a) d[a] = d[a] - sp.box[a] * rintf(d[a] * sp.inv_box[a]);
+          float dsq = d[0] * d[0] + d[1] * d[1];
+          if (DIM == 3) dsq = dsq + d[2] * d[2];
+          float R = pi.w + pj.w;
+          if (dsq < R * R) {
+            if (pass == 1 && o + c < cap) {
+              pairs[2 * (o + c)] = oi;
+              pairs[2 * (o + c) + 1] = oj;
+            }
+            ++c;
+          }
+        }
+      }
+    }
+  if (pass == 0) counts[t] = c;
+}
+
+// ------------------------------------------------------------- launchers
+
+static inline unsigned int nblk(long long n, int t) { return (unsigned int)((n + t - 1) / t); }
+
+void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, const float* frc,
+                 const float* rad, const float* mass, const int32_t* mat, const uint8_t* fixed,
+                 const int32_t* sys_of, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_pack<3><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc, rad, mass, mat, fixed, sys_of);
+  else k_pack<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc, rad, mass, mat, fixed, sys_of);
+}
+
+void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_unpack<3><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc);
+  else k_unpack<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc);
+}
+
+void launch_scan(const Bufs& b, cudaStream_t st) {
+  unsigned int nb = nblk(b.C, SCAN_TILE);
+  k_scan_reduce<<<nb, SCAN_T, 0, st>>>(b);
+  k_scan_top<<<1, 1024, 0, st>>>(b, (int)nb);
+  k_scan_down<<<nb, SCAN_T, 0, st>>>(b);
+}
+
+void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (any_free) {
+    if (dim == 3) k_grid_free<3><<<b.S, 256, 0, st>>>(b);
+    else k_grid_free<2><<<b.S, 256, 0, st>>>(b);
+  }
+  if (dim == 3) k_bin<3><<<nblk(b.P, 256), 256, 0, st>>>(b);
+  else k_bin<2><<<nblk(b.P, 256), 256, 0, st>>>(b);
+  launch_scan(b, st);
+  k_scatter<<<nblk(b.P, 256), 256, 0, st>>>(b);
+  k_cellsort<<<nblk(b.C, 256), 256, 0, st>>>(b);
+  k_gather<<<nblk(b.P, 256), 256, 0, st>>>(b);
+}
+
+int rebuild_kernel_count(bool any_free) { return any_free ? 8 : 7; }
+
+void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_pre<3><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  else k_pre<2><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+}
+
+void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_force<3><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  else k_force<2><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+}
+
+void launch_rot(int dim, const Bufs& b, const int32_t* sys_of, float4* q, float* angv, float* torque,
+                const float* inertia, const uint8_t* fixed, long long nsteps, cudaStream_t st) {
+  if (b.P == 0 || nsteps == 0) return;
+  if (dim == 3) k_rot<3><<<nblk(b.P, 256), 256, 0, st>>>(b, sys_of, q, angv, torque, inertia, fixed, nsteps);
+  else k_rot<2><<<nblk(b.P, 256), 256, 0, st>>>(b, sys_of, q, angv, torque, inertia, fixed, nsteps);
+}
+
+void launch_ke_rot(int dim, long long N, const float4* q, const float* angv, const float* inertia,
+                   double* out, cudaStream_t st) {
+  if (N == 0) return;
+  if (dim == 3) k_ke_rot<3><<<nblk(N, 256), 256, 0, st>>>(N, q, angv, inertia, out);
+  else k_ke_rot<2><<<nblk(N, 256), 256, 0, st>>>(N, q, angv, inertia, out);
+}
+
+void launch_energy(int dim, const Bufs& b, double* out, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_energy<3><<<nblk(b.P, 256), 256, 0, st>>>(b, out);
+  else k_energy<2><<<nblk(b.P, 256), 256, 0, st>>>(b, out);
+}
+
+
+void launch_contacts(int dim, const Bufs& b, int pass, int32_t* counts, const long long* offs,
+                     int32_t* pairs, long long cap, cudaStream_t st) {
+  if (b.P == 0) return;
+  if (dim == 3) k_contacts<3><<<nblk(b.P, 256), 256, 0, st>>>(b, pass, counts, offs, pairs, cap);
+  else k_contacts<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pass, counts, offs, pairs, cap);
+}
+
+}  // namespace jdem

@@ -1,0 +1,24 @@
+// Host-side launchers of the engine kernels (jdem_kernels.cu).
+#pragma once
+#include "jdem_device.cuh"
+
+namespace jdem {
+
+void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, const float* frc,
+                 const float* rad, const float* mass, const int32_t* mat, const uint8_t* fixed,
+                 const int32_t* sys_of, cudaStream_t st);
+void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st);
+void launch_scan(const Bufs& b, cudaStream_t st);
+void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
+int rebuild_kernel_count(bool any_free);
+void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_rot(int dim, const Bufs& b, const int32_t* sys_of, float4* q, float* angv, float* torque,
+                const float* inertia, const uint8_t* fixed, long long nsteps, cudaStream_t st);
+void launch_ke_rot(int dim, long long N, const float4* q, const float* angv, const float* inertia,
+                   double* out, cudaStream_t st);
+void launch_energy(int dim, const Bufs& b, double* out, cudaStream_t st);
+void launch_contacts(int dim, const Bufs& b, int pass, int32_t* counts, const long long* offs,
+                     int32_t* pairs, long long cap, cudaStream_t st);
+
+}  // namespace jdem

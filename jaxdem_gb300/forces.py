@@ -1,0 +1,74 @@
+"""Force model and force manager (``jaxdem/forces``).
+
+``SpringForce`` (``forces/spring.py:69-147``) is evaluated on the device by
+the collider kernels; this class carries its identity and material
+requirements.  ``ForceManager`` (``forces/force_manager.py``) carries gravity
+and the per-step external buffers; the device applies gravity
+(``force_manager.py:393-397``) inside the fused step kernel.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any, Sequence
+
+import numpy as np
+
+from .factory import Factory
+
+F32 = np.float32
+
+
+class ForceModel(Factory):
+    @property
+    def required_material_properties(self) -> tuple:
+        return ()
+
+    @property
+    def requires_history(self) -> bool:
+        return False
+
+
+@ForceModel.register("spring")
+@dataclass
+class SpringForce(ForceModel):
+    """Linear normal spring: F = k max(0, Ri + Rj - r) r_hat, E = k delta^2 / 2."""
+
+    @property
+    def required_material_properties(self) -> tuple:
+        return ("young_eff",)
+
+
+@dataclass
+class ForceManager:
+    gravity: np.ndarray
+    external_force: np.ndarray
+    external_force_com: np.ndarray
+    external_torque: np.ndarray
+    force_functions: tuple = ()
+    energy_functions: tuple = ()
+    is_com_force: tuple = ()
+
+    @staticmethod
+    def create(state_shape: Sequence[int], *, gravity=None, force_functions: Sequence[Any] = ()) -> "ForceManager":
+        """``ForceManager.create`` (``force_manager.py:80-190``)."""
+        dim = state_shape[-1]
+        g = np.zeros(dim, F32) if gravity is None else np.asarray(gravity, F32)
+        ad = 1 if dim == 2 else 3
+        funcs = tuple(f if isinstance(f, (tuple, list)) else (f,) for f in force_functions)
+        return ForceManager(gravity=g, external_force=np.zeros(tuple(state_shape), F32),
+                            external_force_com=np.zeros(tuple(state_shape), F32),
+                            external_torque=np.zeros((*tuple(state_shape)[:-1], ad), F32),
+                            force_functions=tuple(f[0] for f in funcs),
+                            energy_functions=tuple(f[1] if len(f) > 1 and callable(f[1]) else None for f in funcs),
+                            is_com_force=tuple(bool(f[-1]) if isinstance(f[-1], bool) else False for f in funcs))
+
+    @staticmethod
+    def add_force(state, system, force, *, is_com: bool = False):
+        """Accumulate a one-step external force (``force_manager.py:192-``)."""
+        fm = system.force_manager
+        if is_com:
+            fm.external_force_com = (fm.external_force_com + np.asarray(force, F32)).astype(F32)
+        else:
+            fm.external_force = (fm.external_force + np.asarray(force, F32)).astype(F32)
+        return system
