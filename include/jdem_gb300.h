@@ -185,6 +185,23 @@ int jdem_stats(JdemHandle* h, JdemStats* out);
 /* cudaStream_t the handle launches on (as void*). */
 void* jdem_stream(JdemHandle* h);
 
+/* Contact forces of one sphere system from caller-owned device buffers, without
+ * allocating device memory.  No counterpart in the reference: it exists for callers
+ * that may not call cudaMalloc while they run, such as an XLA FFI handler (XLA owns
+ * and preallocates the device memory pool) or code inside another framework's
+ * memory budget.  Scratch lives in one fixed device array per GPU, held until exit;
+ * n is limited to JDEM_NOALLOC_MAX_PARTICLES (larger n: JDEM_ERR_CAPACITY_OVERFLOW)
+ * and the grid is coarsened to JDEM_NOALLOC_MAX_CELLS cells.  Calls that overlap on
+ * the GPU race on that array.  The first call on a device resolves the array's
+ * address and must come before any stream capture.  pos (n, dim), rad (n) and force
+ * (n, dim) are device pointers; box_size/anchor are host arrays of dim floats;
+ * young is the spring stiffness; work is queued on stream without waiting. */
+#define JDEM_NOALLOC_MAX_PARTICLES 65536
+#define JDEM_NOALLOC_MAX_CELLS 131072
+int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain, const float* box_size,
+                               const float* anchor, float young, const float* pos, const float* rad,
+                               float* force, void* stream);
+
 /* Page-lock caller host memory for asynchronous copies (cudaHostRegister). */
 int jdem_host_register(void* ptr, size_t bytes);
 int jdem_host_unregister(void* ptr);
