@@ -84,6 +84,8 @@ typedef struct {
   int32_t interact_same_bond_id;/* System.interact_same_bond_id */
   int32_t chunk_steps;          /* steps per captured CUDA graph (<= 0: 50) */
   int32_t device;               /* CUDA device ordinal */
+  int32_t neighbor_list;        /* Verlet list built at each re-sort: 0 = on (capacity from the
+                                   density), > 0 = on with this initial capacity, -1 = off */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

@@ -71,6 +71,7 @@ class Config(C.Structure):
         ("interact_same_bond_id", C.c_int32),
         ("chunk_steps", C.c_int32),
         ("device", C.c_int32),
+        ("neighbor_list", C.c_int32),
     ]
 
 
@@ -172,7 +173,7 @@ class Engine:
 
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
-                 device: int = 0):
+                 device: int = 0, neighbor_list=True):
         self.lib = load()
         self.dim = int(dim)
         self.n_per_system = [int(s["n"]) for s in systems]
@@ -211,6 +212,10 @@ class Engine:
         cfg.interact_same_bond_id = int(bool(interact_same_bond_id))
         cfg.chunk_steps = int(chunk_steps)
         cfg.device = int(device)
+        # True: list with automatic capacity; False: cell traversal every step;
+        # an int > 0: list with that initial capacity
+        cfg.neighbor_list = (-1 if neighbor_list is False else
+                             (0 if neighbor_list is True else int(neighbor_list)))
         self._descs = descs
         h = C.c_void_p()
         rc = self.lib.jdem_create(C.byref(cfg), C.byref(h))

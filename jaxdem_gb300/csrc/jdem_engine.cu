@@ -18,6 +18,9 @@ using namespace jdem;
 
 namespace {
 
+// largest Verlet-list row the list build can stage in shared memory
+constexpr int kMaxListCap = 384;
+
 const char* kStatusNames[] = {"ok",          "bad argument", "capacity overflow", "hash overflow",
                               "non-finite state", "out of device memory", "timeout",
                               "unsupported configuration", "CUDA error", "not ready"};
@@ -50,7 +53,9 @@ void JdemHandle::free_all() {
   if (h_status) cudaFreeHost(h_status);
   h_status = nullptr;
   if (own_stream && stream) cudaStreamDestroy(stream);
+  if (side) cudaStreamDestroy(side);
   stream = nullptr;
+  side = nullptr;
   for (auto& e : ev_pool) cudaEventDestroy(e);
   ev_pool.clear();
 }
@@ -144,6 +149,8 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   n_mat = cfg->n_materials;
   bond_w = cfg->bond_width;
   interact_same_bond = cfg->interact_same_bond_id;
+  use_nl = cfg->neighbor_list >= 0;
+  nl_request = cfg->neighbor_list;
   desc.assign(cfg->systems, cfg->systems + S);
   P = 0;
   for (int s = 0; s < S; ++s) {
@@ -163,6 +170,7 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   }
   if (P >= (1LL << 31) - 1) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "more than 2^31-2 particles");
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   own_stream = true;
   JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, 64));
   int rc;
@@ -287,6 +295,49 @@ int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
   }
   JDEM_CUDA_TRY(this, cudaMemsetAsync(b.cnt, 0, sizeof(int32_t) * (size_t)C, stream));
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.sys, sys_h.data(), sizeof(SysParams) * S, cudaMemcpyHostToDevice, stream));
+  if (!use_nl) return plan_list(0);
+  // Verlet-list capacity: expected neighbours within 2 r_max + skin at the
+  // densest system, plus eight standard deviations of a Poisson count.
+  double mean_max = 0.0;
+  off = 0;
+  for (int s = 0; s < S; ++s) {
+    const SysParams& sp = sys_h[s];
+    double vol = 1.0, rl = 0.0;
+    float rmax = 0.0f;
+    for (long long i = off; i < off + desc[s].n; ++i) rmax = std::max(rmax, rad_h[i]);
+    rl = 2.0 * rmax + skin;
+    for (int a = 0; a < dim; ++a)
+      vol *= sp.domain == DOM_FREE ? std::max(1e-30, (double)sp.g[a] * (double)sp.gcell[a]) : (double)sp.box[a];
+    double sphere = dim == 3 ? 4.18879 * rl * rl * rl : 3.14159 * rl * rl;
+    double mean = desc[s].n / vol * sphere;
+    mean_max = std::max(mean_max, mean);
+    off += desc[s].n;
+  }
+  int cap = (int)std::ceil(mean_max + 8.0 * std::sqrt(mean_max) + 16.0);
+  cap = std::min(256, (cap + 7) / 8 * 8);
+  if (nl_request > 0) cap = nl_request;
+  return plan_list(cap);
+}
+
+// (Re)allocate the Verlet list for cap entries per slot (0: no list).
+int JdemHandle::plan_list(int cap) {
+  if (cap == b.nl_cap && (cap == 0 || b.nbr)) return JDEM_OK;
+  drop_graphs();
+  dfree(b.nbr);
+  dfree(b.ncnt);
+  b.nbr = nullptr;
+  b.ncnt = nullptr;
+  b.nl_cap = 0;
+  b.nl_skin = skin;
+  if (cap <= 0 || P == 0) return JDEM_OK;
+  cap = std::min(cap, kMaxListCap);
+  if (prepare_nlbuild(cap)) return fail(JDEM_ERR_CUDA, "cannot raise shared memory for the list build");
+  int rc;
+  // sliced layout: one cap x 32 block per warp of slots
+  size_t slices = (size_t)((P + 31) / 32);
+  if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)cap * 32 * slices))) return rc;
+  if ((rc = dalloc((void**)&b.ncnt, sizeof(int32_t) * (size_t)P))) return rc;
+  b.nl_cap = cap;
   return JDEM_OK;
 }
 
@@ -411,7 +462,54 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
 // fused force kernel.
 void JdemHandle::enqueue_step(int mode) {
   launch_rebuild(dim, b, any_free, stream);
+  launch_nlbuild(dim, b, stream);
   launch_force(dim, b, mode, stream);
+  launch_fin(b, true, false, 0, stream);
+}
+
+// Conditional handle on the graph being captured on `stream`.
+int JdemHandle::capture_handle(cudaGraphConditionalHandle* hc) {
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cg;
+  JDEM_CUDA_TRY(this, cudaStreamGetCaptureInfo(stream, &cst, nullptr, &cg, nullptr, nullptr, nullptr));
+  JDEM_CUDA_TRY(this, cudaGraphConditionalHandleCreate(hc, cg, 0, cudaGraphCondAssignDefault));
+  return JDEM_OK;
+}
+
+// One step inside a stream capture: the re-sort and list-build kernels form
+// the body of a conditional node whose condition the previous k_fin (or, for
+// the first step, k_cond) sets from the device flags, so a step without a
+// re-sort launches two kernels (k_force, k_fin).
+int JdemHandle::capture_step_conditional(int mode, cudaGraphConditionalHandle hc,
+                                         cudaGraphConditionalHandle* next) {
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cg;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  JDEM_CUDA_TRY(this, cudaStreamGetCaptureInfo(stream, &cst, nullptr, &cg, &deps, nullptr, &nd));
+  cudaGraphNodeParams prm = {cudaGraphNodeTypeConditional};
+  prm.type = cudaGraphNodeTypeConditional;
+  prm.conditional.handle = hc;
+  prm.conditional.type = cudaGraphCondTypeIf;
+  prm.conditional.size = 1;
+  cudaGraphNode_t node;
+  JDEM_CUDA_TRY(this, cudaGraphAddNode(&node, cg, deps, nullptr, nd, &prm));
+  cudaGraph_t body = prm.conditional.phGraph_out[0];
+  JDEM_CUDA_TRY(this, cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  launch_rebuild(dim, b, any_free, side);
+  launch_nlbuild(dim, b, side);
+  cudaGraph_t body_out;
+  JDEM_CUDA_TRY(this, cudaStreamEndCapture(side, &body_out));
+  JDEM_CUDA_TRY(this, cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  launch_force(dim, b, mode, stream);
+  if (next) {
+    int rc = capture_handle(next);
+    if (rc) return rc;
+    launch_fin(b, true, true, *next, stream);
+  } else {
+    launch_fin(b, true, false, 0, stream);
+  }
+  return JDEM_OK;
 }
 
 int JdemHandle::run_graph(long long nsteps, int mode_last) {
@@ -419,15 +517,39 @@ int JdemHandle::run_graph(long long nsteps, int mode_last) {
   long long key = nsteps * 64 + mode_last;
   auto it = graphs.find(key);
   if (it == graphs.end()) {
-    cudaGraph_t g;
-    JDEM_CUDA_TRY(this, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (long long k = 0; k < nsteps; ++k) enqueue_step(k + 1 == nsteps ? mode_last : MODE_STEP);
-    cudaError_t e = cudaStreamEndCapture(stream, &g);
-    if (e != cudaSuccess) return fail(JDEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    cudaGraphExec_t ge;
-    e = cudaGraphInstantiate(&ge, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(JDEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ge = nullptr;
+    for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
+      bool cond = use_conditional && attempt == 0;
+      cudaGraph_t g = nullptr;
+      JDEM_CUDA_TRY(this, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      int rc = JDEM_OK;
+      cudaGraphConditionalHandle hc = 0;
+      if (cond) {
+        rc = capture_handle(&hc);
+        if (rc == JDEM_OK) launch_cond(b, hc, stream);
+      }
+      for (long long k = 0; k < nsteps && rc == JDEM_OK; ++k) {
+        int m = k + 1 == nsteps ? mode_last : MODE_STEP;
+        if (cond) {
+          cudaGraphConditionalHandle nx = 0;
+          rc = capture_step_conditional(m, hc, k + 1 < nsteps ? &nx : nullptr);
+          hc = nx;
+        } else {
+          enqueue_step(m);
+        }
+      }
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (rc == JDEM_OK && e == cudaSuccess) {
+        e = cudaGraphInstantiate(&ge, g, 0);
+        if (e != cudaSuccess) ge = nullptr;
+      }
+      if (g) cudaGraphDestroy(g);
+      if (!ge) {
+        cudaGetLastError();
+        if (!cond) return fail(JDEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        use_conditional = false;  // fall back to unconditional re-sort launches
+      }
+    }
     it = graphs.emplace(key, ge).first;
   }
   JDEM_CUDA_TRY(this, cudaGraphLaunch(it->second, stream));
@@ -484,8 +606,20 @@ int JdemHandle::sync_status() {
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(h_status, b.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
   JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
   const Ctl* c = (const Ctl*)h_status;
-  sticky_status |= c->status;
+  sticky_status |= c->status & ~(unsigned int)ST_NL_OVERFLOW;
   rebuilds = c->rebuilds;
+  if (c->status & ST_NL_OVERFLOW) {
+    // a list row overflowed: those steps used the cell traversal (still
+    // exact); double the capacity and rebuild the list before the next step
+    int grown = std::min(kMaxListCap, std::max(16, 2 * b.nl_cap));
+    int rc = grown > b.nl_cap ? plan_list(grown) : JDEM_OK;
+    if (rc) return rc;
+    unsigned int st = c->status & ~(unsigned int)ST_NL_OVERFLOW, one = 1u;
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->status, &st, 4, cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->nl_dirty, &one, 4, cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    nl_regrowths += 1;
+  }
   if (bbox_pending) {
     // FreeDomain.apply of the last step: box = max - min, anchor = min (free.py:59-63)
     std::vector<unsigned int> bb((size_t)S * 6);
@@ -529,9 +663,11 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
   launch_pre(dim, b, 0, stream);
   for (long long k = 0; k < n; ++k) {
     launch_rebuild(dim, b, any_free, stream);
+    launch_nlbuild(dim, b, stream);
     JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[2 + 2 * k], stream));
     launch_force(dim, b, k + 1 == n ? MODE_STEP_LAST : MODE_STEP, stream);
     JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[3 + 2 * k], stream));
+    launch_fin(b, true, false, 0, stream);
   }
   if (rot_active) launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
   JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[1], stream));
@@ -576,6 +712,7 @@ int JdemHandle::compute_force() {
   if (P == 0) return JDEM_OK;
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
   launch_rebuild(dim, b, any_free, stream);
+  launch_nlbuild(dim, b, stream);
   launch_force(dim, b, MODE_FORCE_ONLY, stream);
   int ad = dim == 3 ? 3 : 1;
   JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));

@@ -22,6 +22,8 @@ struct JdemHandle {
   std::vector<JdemSystemDesc> desc;
   std::vector<jdem::SysParams> sys_h;
   bool any_free = false;
+  bool use_nl = true;
+  int nl_request = 0;
   bool rot_active = false;
   bool uploaded = false;
   bool bbox_pending = false;
@@ -40,6 +42,8 @@ struct JdemHandle {
 
   // runtime
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;     // captures the conditional re-sort bodies
+  bool use_conditional = true;
   bool own_stream = false;
   void* h_status = nullptr;
   std::map<long long, cudaGraphExec_t> graphs;
@@ -49,6 +53,7 @@ struct JdemHandle {
   long long device_bytes = 0;
   long long steps_done = 0;
   long long rebuilds = 0;
+  long long nl_regrowths = 0;
   unsigned int sticky_status = 0;
   std::string err;
 
@@ -59,9 +64,12 @@ struct JdemHandle {
   void drop_graphs();
   int setup(const JdemConfig* cfg);
   int plan_cells(const float* rad_h, const float* pos_h);
+  int plan_list(int cap);
   int reset_ctl();
   int upload(const JdemHostState* s, bool device_ptrs);
   void enqueue_step(int mode);
+  int capture_handle(cudaGraphConditionalHandle* hc);
+  int capture_step_conditional(int mode, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle* next);
   int run_graph(long long nsteps, int mode_last);
   int step_async(long long n);
   int sync_status();

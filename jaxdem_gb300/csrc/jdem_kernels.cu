@@ -28,37 +28,35 @@ __device__ __forceinline__ T warp_max(T v) {
   return v;
 }
 
-// Block max of a non-negative float, then one atomicMax per block; the last
-// block to finish folds the kernel's maximum into the displacement bound and
-// raises need_rebuild.  No thread waits on another.
-__device__ void finish_displacement(Ctl* ctl, float d2, bool flip_pos) {
-  __shared__ float red[32];
-  __shared__ bool is_last;
+// Warp max of the squared displacement; lane 0 raises the kernel-wide
+// maximum only when it exceeds the value already recorded, so the atomic is
+// rare.  No thread waits on another; k_fin folds the maximum in afterwards.
+__device__ __forceinline__ void warp_disp(Ctl* ctl, float d2) {
   d2 = warp_max(d2);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) red[wid] = d2;
-  __syncthreads();
-  if (wid == 0) {
-    int nw = (blockDim.x + 31) >> 5;
-    float v = lane < nw ? red[lane] : 0.0f;
-    v = warp_max(v);
-    if (lane == 0) {
-      if (v > 0.0f) atomicMax(&ctl->maxdisp2, __float_as_uint(v));
-      __threadfence();
-      unsigned int prev = atomicAdd(&ctl->done, 1u);
-      is_last = (prev == gridDim.x - 1);
-    }
+  if ((threadIdx.x & 31) == 0 && d2 > 0.0f && d2 > __uint_as_float(__ldcg(&ctl->maxdisp2)))
+    atomicMax(&ctl->maxdisp2, __float_as_uint(d2));
+}
+
+// After a kernel that moved particles: bound += max displacement, raise
+// need_rebuild past skin / 2; after a force kernel also flip the position
+// buffer and retire the list-build request.  Inside a captured step it sets
+// the condition of the next step's re-sort body.
+enum : int { FIN_AFTER_FORCE = 1, FIN_SET_COND = 2 };
+
+__global__ void k_fin(Ctl* ctl, int flags, cudaGraphConditionalHandle h) {
+  float m2 = __uint_as_float(atomicExch(&ctl->maxdisp2, 0u));
+  float bd = ctl->bound + sqrtf(m2);
+  ctl->bound = bd;
+  unsigned int nr = ctl->need_rebuild;
+  if (bd > ctl->skin_half) nr = 1u;
+  ctl->need_rebuild = nr;
+  unsigned int nd = ctl->nl_dirty;
+  if (flags & FIN_AFTER_FORCE) {
+    ctl->pos_sel ^= 1u;
+    nd = 0u;
+    ctl->nl_dirty = 0u;
   }
-  __syncthreads();
-  if (is_last && threadIdx.x == 0) {
-    __threadfence();
-    float m2 = __uint_as_float(atomicExch(&ctl->maxdisp2, 0u));
-    float b = ctl->bound + sqrtf(m2);
-    ctl->bound = b;
-    if (b > ctl->skin_half) ctl->need_rebuild = 1u;
-    if (flip_pos) ctl->pos_sel ^= 1u;
-    ctl->done = 0u;
-  }
+  if (flags & FIN_SET_COND) cudaGraphSetConditional(h, (nr | nd) ? 1u : 0u);
 }
 
 // ------------------------------------------------------------ pack / unpack
@@ -324,7 +322,8 @@ __global__ void k_gather(Bufs b) {
     int t = b.perm_tmp[u];
     b.pos[ps ^ 1u][u] = b.pos[ps][t];
     b.vel[sel ^ 1u][u] = b.vel[sel][t];
-    b.frc[sel ^ 1u][u] = b.frc[sel][t];
+    // forces are not moved: every re-sort is followed by a force kernel that
+    // rewrites frc for all slots before anything reads it
     b.tag[sel ^ 1u][u] = b.tag[sel][t];
     b.orig[sel ^ 1u][u] = b.orig[sel][t];
     b.key[sel ^ 1u][u] = b.key_tmp[t];
@@ -341,6 +340,7 @@ __global__ void k_gather(Bufs b) {
     b.ctl->sel = sel ^ 1u;
     b.ctl->pos_sel = ps ^ 1u;
     b.ctl->need_rebuild = 0u;
+    b.ctl->nl_dirty = 1u;
     b.ctl->bound = 0.0f;
     b.ctl->rebuilds += 1u;
     b.ctl->done2 = 0u;
@@ -395,33 +395,105 @@ __global__ void k_pre(Bufs b, int mode) {
       d2 = 0.0f;
     }
   }
-  finish_displacement(b.ctl, d2, false);
+  warp_disp(b.ctl, d2);
 }
 
 // ---------------------------------------------------------- fused step
 
-// One thread per slot.  Contact force (spring.py:97-108 with the periodic
-// minimum image of periodic.py:74-79) summed over the stencil, then
-// ForceManager gravity (force_manager.py:393-405), step_after_force, and, in
-// MODE_STEP, the next step's ReflectDomain.apply, step_before_force and drift.
+// Visit every slot binned in the unique stencil cells of a slot's cell
+// (cell_list.py:66-96 stencil, deduplicated for small periodic grids).  The
+// three cells of a stencil row along x form at most two contiguous slot ranges.
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_candidate(const int32_t* __restrict__ cs, const SysParams& sp,
+                                                   long long local, F&& f) {
+  const bool per = sp.domain == DOM_PERIODIC;
+  const int gx = sp.g[0], gy = sp.g[1];
+  int cx = (int)(local % gx);
+  long long rem = local / gx;
+  int cy = (int)(rem % gy);
+  int cz = DIM == 3 ? (int)(rem / gy) : 0;
+  int ys[3], zs[3];
+  int ny = axis_set(cy, gy, per, ys);
+  int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
+  if (DIM == 2) zs[0] = 0;
+  int xa0, xb0, xa1, xb1;
+  x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
+  for (int iz = 0; iz < nz; ++iz) {
+    for (int iy = 0; iy < ny; ++iy) {
+      long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
+      int ja = cs[row + xa0], jb = cs[row + xb0];
+      for (int j = ja; j < jb; ++j) f(j);
+      if (xa1 < xb1) {
+        ja = cs[row + xa1];
+        jb = cs[row + xb1];
+        for (int j = ja; j < jb; ++j) f(j);
+      }
+    }
+  }
+}
+
+// Minimum-image displacement and squared distance, in the reference's order.
 template <int DIM>
-__global__ void __launch_bounds__(256) k_force(Bufs b, int mode) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  int base_mode = mode & 7;
-  float d2max = 0.0f;
-  if (t < b.P) {
-    const float4* __restrict__ P = b.pos[ps];
+__device__ __forceinline__ float pair_disp(const SysParams& sp, bool per, float4 pi, float4 pj, float& dx,
+                                           float& dy, float& dz) {
+  dx = pi.x - pj.x;
+  dy = pi.y - pj.y;
+  dz = DIM == 3 ? pi.z - pj.z : 0.0f;
+  if (per) {
+    dx = dx - sp.box[0] * rintf(dx * sp.inv_box[0]);
+    dy = dy - sp.box[1] * rintf(dy * sp.inv_box[1]);
+    if (DIM == 3) dz = dz - sp.box[2] * rintf(dz * sp.inv_box[2]);
+  }
+  float dsq = dx * dx + dy * dy;
+  if (DIM == 3) dsq = dsq + dz * dz;
+  return dsq;
+}
+
+// Verlet list of every slot, built right after a re-sort: all j with
+// |r_ij| < r_i + r_j + skin.  While the displacement bound stays below
+// skin / 2 every contact of the following steps is in the list.  One thread
+// per slot walks its stencil ranges four candidates at a time (independent
+// loads); entries go to the sliced layout nbr[((t / 32) * cap + k) * 32 +
+// t % 32], so a warp writes, and the force kernel reads, one coalesced row
+// per k.  Entries are in ascending slot order within each stencil row.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
+  if (ld_cg_u32(&b.ctl->nl_dirty) == 0u) return;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  const float4* __restrict__ P = b.pos[ps];
+  const float4 pi = P[t];
+  const SysParams& sp = b.sys[b.tag[sel][t] & TAG_SYS_MASK];
+  const bool per = sp.domain == DOM_PERIODIC;
+  const float skin = b.nl_skin;
+  const int cap = b.nl_cap;
+  int32_t* __restrict__ out = b.nbr + ((t >> 5) * cap) * 32 + (t & 31);
+  int n = 0;
+  auto range = [&](int ja, int jb) {
+    for (int j = ja; j < jb; j += 4) {
+      float4 q[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = j + u < jb ? P[j + u] : pi;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int jj = j + u;
+        if (jj < jb && jj != (int)t) {
+          float dx, dy, dz;
+          float dsq = pair_disp<DIM>(sp, per, pi, q[u], dx, dy, dz);
+          float rc = pi.w + q[u].w + skin;
+          if (dsq < rc * rc) {
+            if (n < cap) out[n * 32] = jj;
+            ++n;
+          }
+        }
+      }
+    }
+  };
+  {
     const int32_t* __restrict__ cs = b.cell_start;
-    float4 pi = P[t];
-    uint32_t tg = b.tag[sel][t];
-    int s = tg & TAG_SYS_MASK;
-    const SysParams& sp = b.sys[s];
-    const bool per = sp.domain == DOM_PERIODIC;
-    const float bx = sp.box[0], by = sp.box[1], bz = sp.box[2];
-    const float ibx = sp.inv_box[0], iby = sp.inv_box[1], ibz = sp.inv_box[2];
+    const long long local = b.key[sel][t] - sp.c0;
     const int gx = sp.g[0], gy = sp.g[1];
-    long long local = b.key[sel][t] - sp.c0;
     int cx = (int)(local % gx);
     long long rem = local / gx;
     int cy = (int)(rem % gy);
@@ -432,56 +504,92 @@ __global__ void __launch_bounds__(256) k_force(Bufs b, int mode) {
     if (DIM == 2) zs[0] = 0;
     int xa0, xb0, xa1, xb1;
     x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
+    for (int iz = 0; iz < nz; ++iz)
+      for (int iy = 0; iy < ny; ++iy) {
+        long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
+        range(cs[row + xa0], cs[row + xb0]);
+        if (xa1 < xb1) range(cs[row + xa1], cs[row + xb1]);
+      }
+  }
+  if (n > cap) {
+    atomicOr(&b.ctl->status, ST_NL_OVERFLOW);
+    n = cap;
+  }
+  b.ncnt[t] = n;
+}
+
+// Sets the condition of the re-sort body of a captured step.
+__global__ void k_cond(const Ctl* ctl, cudaGraphConditionalHandle h) {
+  unsigned int v = __ldcg(&ctl->need_rebuild) | __ldcg(&ctl->nl_dirty);
+  cudaGraphSetConditional(h, v ? 1u : 0u);
+}
+
+// One thread per slot.  Contact force (spring.py:97-108 with the periodic
+// minimum image of periodic.py:74-79), from the Verlet list when NL is set
+// and the list is complete, else from the stencil cells; then ForceManager
+// gravity (force_manager.py:393-405), step_after_force, and, in MODE_STEP,
+// the next step's ReflectDomain.apply, step_before_force and drift.
+template <int DIM, bool NL>
+__global__ void __launch_bounds__(256, 4) k_force(Bufs b, int mode) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  const bool use_list = NL && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  int base_mode = mode & 7;
+  float d2max = 0.0f;
+  if (t < b.P) {
+    const float4* __restrict__ P = b.pos[ps];
+    const float4 pi = P[t];
+    const uint32_t tg = b.tag[sel][t];
+    const int s = tg & TAG_SYS_MASK;
+    const SysParams& sp = b.sys[s];
+    const bool per = sp.domain == DOM_PERIODIC;
     const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
     const float k0 = b.young[mat_i * b.n_mat + mat_i];
     const bool multi_mat = b.n_mat > 1;
-    const bool bonds = b.bond_w > 0;
+    const bool bonds = b.bond_w > 0 && !b.interact_same_bond;
     const int oi = bonds ? b.orig[sel][t] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
-    for (int iz = 0; iz < nz; ++iz) {
-      for (int iy = 0; iy < ny; ++iy) {
-        long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
-        for (int r = 0; r < 2; ++r) {
-          int ca = r == 0 ? xa0 : xa1, cb = r == 0 ? xb0 : xb1;
-          if (ca >= cb) continue;
-          int ja = cs[row + ca], jb = cs[row + cb];
-          for (int j = ja; j < jb; ++j) {
-            float4 pj = P[j];
-            float dx = pi.x - pj.x;
-            float dy = pi.y - pj.y;
-            float dz = DIM == 3 ? pi.z - pj.z : 0.0f;
-            if (per) {
-              dx = dx - bx * rintf(dx * ibx);
-              dy = dy - by * rintf(dy * iby);
-              if (DIM == 3) dz = dz - bz * rintf(dz * ibz);
-            }
-            float dsq = dx * dx + dy * dy;
-            if (DIM == 3) dsq = dsq + dz * dz;
-            float R = pi.w + pj.w;
-            if (dsq < R * R * 1.000001f && j != (int)t) {
-              float k = k0;
-              if (multi_mat) {
-                int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
-                k = b.young[mat_i * b.n_mat + mat_j];
-              }
-              if (bonds && !b.interact_same_bond) {
-                int oj = b.orig[sel][j];
-                bool bonded = false;
-                for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
-                if (bonded) continue;
-              }
-              float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
-              float rr = dsq * inv;
-              float delta = R - rr;
-              delta = delta > 0.0f ? delta : 0.0f;
-              float mag = k * delta * inv;
-              two_sum_acc(fx, ex, mag * dx);
-              two_sum_acc(fy, ey, mag * dy);
-              if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
-            }
-          }
+    auto pair = [&](int j, const float4& pj) {
+      float dx, dy, dz;
+      float dsq = pair_disp<DIM>(sp, per, pi, pj, dx, dy, dz);
+      float R = pi.w + pj.w;
+      if (dsq < R * R * 1.000001f && j != (int)t) {
+        float k = k0;
+        if (multi_mat) {
+          int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+          k = b.young[mat_i * b.n_mat + mat_j];
         }
+        if (bonds) {
+          int oj = b.orig[sel][j];
+          bool bonded = false;
+          for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
+          if (bonded) return;
+        }
+        float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
+        float rr = dsq * inv;
+        float delta = R - rr;
+        delta = delta > 0.0f ? delta : 0.0f;
+        float mag = k * delta * inv;
+        two_sum_acc(fx, ex, mag * dx);
+        two_sum_acc(fy, ey, mag * dy);
+        if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
       }
+    };
+    if (use_list) {
+      const int n = b.ncnt[t];
+      const int32_t* __restrict__ nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
+      for (int k = 0; k < n; k += 4) {
+        int jj[4];
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) jj[u] = k + u < n ? nb[(k + u) * 32] : (int)t;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = P[jj[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) pair(jj[u], q[u]);
+      }
+    } else {
+      for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) { pair(j, P[j]); });
     }
     float F[3] = {fx + ex, fy + ey, DIM == 3 ? fz + ez : 0.0f};
     if (base_mode == MODE_FORCE_ONLY) {
@@ -540,7 +648,7 @@ __global__ void __launch_bounds__(256) k_force(Bufs b, int mode) {
       }
     }
   }
-  if (base_mode != MODE_FORCE_ONLY) finish_displacement(b.ctl, d2max, true);
+  if (base_mode != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
 }
 
 // -------------------------------------------------------------- rotation
@@ -886,12 +994,34 @@ void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
   if (dim == 3) k_pre<3><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
   else k_pre<2><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  launch_fin(b, false, false, 0, st);
 }
+
+size_t nlbuild_smem(int cap) { return 0; }
+
+int prepare_nlbuild(int cap) { return 0; }
+
+void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st) {
+  if (b.P == 0 || b.nl_cap <= 0) return;
+  if (dim == 3) k_nlbuild<3><<<nblk(b.P, 256), 256, 0, st>>>(b);
+  else k_nlbuild<2><<<nblk(b.P, 256), 256, 0, st>>>(b);
+}
+
+void launch_fin(const Bufs& b, bool after_force, bool set_cond, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_fin<<<1, 1, 0, st>>>(b.ctl, (after_force ? FIN_AFTER_FORCE : 0) | (set_cond ? FIN_SET_COND : 0), h);
+}
+
+void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st) { k_cond<<<1, 1, 0, st>>>(b.ctl, h); }
 
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
-  if (dim == 3) k_force<3><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
-  else k_force<2><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  if (b.nl_cap > 0) {
+    if (dim == 3) k_force<3, true><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+    else k_force<2, true><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  } else {
+    if (dim == 3) k_force<3, false><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+    else k_force<2, false><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  }
 }
 
 void launch_rot(int dim, const Bufs& b, const int32_t* sys_of, float4* q, float* angv, float* torque,

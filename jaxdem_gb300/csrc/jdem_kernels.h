@@ -13,6 +13,12 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
 int rebuild_kernel_count(bool any_free);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st);
+size_t nlbuild_smem(int cap);
+int prepare_nlbuild(int cap);
+void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st);
+// After k_pre / k_force: fold the displacement into the bound (see k_fin).
+void launch_fin(const Bufs& b, bool after_force, bool set_cond, cudaGraphConditionalHandle h, cudaStream_t st);
 void launch_rot(int dim, const Bufs& b, const int32_t* sys_of, float4* q, float* angv, float* torque,
                 const float* inertia, const uint8_t* fixed, long long nsteps, cudaStream_t st);
 void launch_ke_rot(int dim, long long N, const float4* q, const float* angv, const float* inertia,

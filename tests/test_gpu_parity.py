@@ -282,3 +282,22 @@ def test_rotation_verlet_spiral_matches_oracle():
     assert np.allclose(out["q"], st1.q, atol=2e-6)
     assert np.allclose(out["ang_vel"], st1.ang_vel, rtol=1e-5, atol=1e-5)
     assert np.all(out["torque"] == 0)
+
+
+@pytest.mark.parametrize("nl", [False, 4])
+def test_verlet_list_paths_agree(nl):
+    """Cell traversal every step (nl=False) and a list that overflows its initial
+    capacity of 4 (cell traversal for those steps, then a larger list) match the
+    default list path."""
+    w = small_periodic(N=4096, radii=(0.5, 0.7), phi=0.55)
+    outs = []
+    for mode in (True, nl):
+        eng = Engine(3, [w.desc()], K, skin=0.1, neighbor_list=mode)
+        try:
+            eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+            eng.step(60)
+            outs.append(eng.download())
+        finally:
+            eng.close()
+    assert min_image_diff(outs[1]["pos_c"], outs[0]["pos_c"], w.box_size) <= 1e-5
+    assert force_err(outs[1]["force"], outs[0]["force"]) <= 1e-4
