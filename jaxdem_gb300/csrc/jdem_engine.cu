@@ -337,6 +337,7 @@ int JdemHandle::plan_list(int cap) {
   size_t slices = (size_t)((P + 31) / 32);
   if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)cap * 32 * slices))) return rc;
   if ((rc = dalloc((void**)&b.ncnt, sizeof(int32_t) * (size_t)P))) return rc;
+  if (!b.posw && (rc = dalloc((void**)&b.posw, sizeof(float4) * (size_t)P))) return rc;
   b.nl_cap = cap;
   return JDEM_OK;
 }

@@ -320,7 +320,19 @@ __global__ void k_gather(Bufs b) {
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   if (u < b.P) {
     int t = b.perm_tmp[u];
-    b.pos[ps ^ 1u][u] = b.pos[ps][t];
+    const float4 p = b.pos[ps][t];
+    b.pos[ps ^ 1u][u] = p;
+    if (b.posw) {
+      // positions wrapped into the primary box, for the list build only
+      const SysParams& sp = b.sys[b.tag[sel][t] & TAG_SYS_MASK];
+      float4 w = p;
+      if (sp.domain == DOM_PERIODIC) {
+        w.x = p.x - sp.box[0] * floorf((p.x - sp.anchor[0]) / sp.box[0]);
+        w.y = p.y - sp.box[1] * floorf((p.y - sp.anchor[1]) / sp.box[1]);
+        w.z = p.z - sp.box[2] * floorf((p.z - sp.anchor[2]) / sp.box[2]);
+      }
+      b.posw[u] = w;
+    }
     b.vel[sel ^ 1u][u] = b.vel[sel][t];
     // forces are not moved: every re-sort is followed by a force kernel that
     // rewrites frc for all slots before anything reads it
@@ -461,16 +473,21 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
   if (ld_cg_u32(&b.ctl->nl_dirty) == 0u) return;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  const float4* __restrict__ P = b.pos[ps];
-  const float4 pi = P[t];
+  const unsigned int sel = ld_cg_u32(&b.ctl->sel);
   const SysParams& sp = b.sys[b.tag[sel][t] & TAG_SYS_MASK];
   const bool per = sp.domain == DOM_PERIODIC;
+  // Wrapped positions with one image shift per stencil row (every grid axis
+  // >= 3 cells makes that shift unique); otherwise the minimum image.  The
+  // test only selects list members, so it may round differently from the
+  // force: the cutoff is widened by 1e-4 relative to stay a superset.
+  const bool shifted = per && b.posw && sp.g[0] >= 3 && sp.g[1] >= 3 && (DIM == 2 || sp.g[2] >= 3);
+  const float4* __restrict__ P = shifted ? b.posw : b.pos[ld_cg_u32(&b.ctl->pos_sel)];
+  const float4 pi = P[t];
   const float skin = b.nl_skin;
   const int cap = b.nl_cap;
   int32_t* __restrict__ out = b.nbr + ((t >> 5) * cap) * 32 + (t & 31);
   int n = 0;
-  auto range = [&](int ja, int jb) {
+  auto range = [&](int ja, int jb, float sx, float sy, float sz) {
     for (int j = ja; j < jb; j += 4) {
       float4 q[4];
 #pragma unroll
@@ -479,9 +496,19 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
       for (int u = 0; u < 4; ++u) {
         const int jj = j + u;
         if (jj < jb && jj != (int)t) {
-          float dx, dy, dz;
-          float dsq = pair_disp<DIM>(sp, per, pi, q[u], dx, dy, dz);
-          float rc = pi.w + q[u].w + skin;
+          float dsq;
+          if (shifted) {
+            float dx = (pi.x - q[u].x) + sx, dy = (pi.y - q[u].y) + sy;
+            dsq = __fmaf_rn(dy, dy, dx * dx);
+            if (DIM == 3) {
+              float dz = (pi.z - q[u].z) + sz;
+              dsq = __fmaf_rn(dz, dz, dsq);
+            }
+          } else {
+            float dx, dy, dz;
+            dsq = pair_disp<DIM>(sp, per, pi, q[u], dx, dy, dz);
+          }
+          float rc = (pi.w + q[u].w + skin) * 1.0001f;
           if (dsq < rc * rc) {
             if (n < cap) out[n * 32] = jj;
             ++n;
@@ -493,23 +520,28 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
   {
     const int32_t* __restrict__ cs = b.cell_start;
     const long long local = b.key[sel][t] - sp.c0;
-    const int gx = sp.g[0], gy = sp.g[1];
+    const int gx = sp.g[0], gy = sp.g[1], gz = sp.g[2];
     int cx = (int)(local % gx);
     long long rem = local / gx;
     int cy = (int)(rem % gy);
     int cz = DIM == 3 ? (int)(rem / gy) : 0;
     int ys[3], zs[3];
     int ny = axis_set(cy, gy, per, ys);
-    int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
+    int nz = DIM == 3 ? axis_set(cz, gz, per, zs) : 1;
     if (DIM == 2) zs[0] = 0;
     int xa0, xb0, xa1, xb1;
     x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
-    for (int iz = 0; iz < nz; ++iz)
+    // image shifts (only used when `shifted`)
+    const float sxw = cx == 0 ? sp.box[0] : -sp.box[0];
+    for (int iz = 0; iz < nz; ++iz) {
+      const float sz = (DIM == 3 && shifted) ? (zs[iz] == gz - 1 && cz == 0 ? sp.box[2] : (zs[iz] == 0 && cz == gz - 1 ? -sp.box[2] : 0.0f)) : 0.0f;
       for (int iy = 0; iy < ny; ++iy) {
+        const float sy = shifted ? (ys[iy] == gy - 1 && cy == 0 ? sp.box[1] : (ys[iy] == 0 && cy == gy - 1 ? -sp.box[1] : 0.0f)) : 0.0f;
         long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
-        range(cs[row + xa0], cs[row + xb0]);
-        if (xa1 < xb1) range(cs[row + xa1], cs[row + xb1]);
+        range(cs[row + xa0], cs[row + xb0], 0.0f, sy, sz);
+        if (xa1 < xb1) range(cs[row + xa1], cs[row + xb1], shifted ? sxw : 0.0f, sy, sz);
       }
+    }
   }
   if (n > cap) {
     atomicOr(&b.ctl->status, ST_NL_OVERFLOW);
@@ -529,7 +561,7 @@ __global__ void k_cond(const Ctl* ctl, cudaGraphConditionalHandle h) {
 // and the list is complete, else from the stencil cells; then ForceManager
 // gravity (force_manager.py:393-405), step_after_force, and, in MODE_STEP,
 // the next step's ReflectDomain.apply, step_before_force and drift.
-template <int DIM, bool NL>
+template <int DIM, bool NL, bool GENERAL>
 __global__ void __launch_bounds__(256, 4) k_force(Bufs b, int mode) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
@@ -545,8 +577,10 @@ __global__ void __launch_bounds__(256, 4) k_force(Bufs b, int mode) {
     const bool per = sp.domain == DOM_PERIODIC;
     const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
     const float k0 = b.young[mat_i * b.n_mat + mat_i];
-    const bool multi_mat = b.n_mat > 1;
-    const bool bonds = b.bond_w > 0 && !b.interact_same_bond;
+    // GENERAL: several materials or bond exclusions (valid_interaction_mask,
+    // colliders/__init__.py:225-243); otherwise both checks compile away
+    const bool multi_mat = GENERAL && b.n_mat > 1;
+    const bool bonds = GENERAL && b.bond_w > 0 && !b.interact_same_bond;
     const int oi = bonds ? b.orig[sel][t] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
     auto pair = [&](int j, const float4& pj) {
@@ -1015,13 +1049,18 @@ void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st) {
 
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
-  if (b.nl_cap > 0) {
-    if (dim == 3) k_force<3, true><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
-    else k_force<2, true><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+  const bool gen = b.n_mat > 1 || (b.bond_w > 0 && !b.interact_same_bond);
+  const unsigned int g = nblk(b.P, 256);
+#define JDEM_FORCE(D, L, G) k_force<D, L, G><<<g, 256, 0, st>>>(b, mode)
+  const bool nl = b.nl_cap > 0;
+  if (dim == 3) {
+    if (nl) { if (gen) JDEM_FORCE(3, true, true); else JDEM_FORCE(3, true, false); }
+    else { if (gen) JDEM_FORCE(3, false, true); else JDEM_FORCE(3, false, false); }
   } else {
-    if (dim == 3) k_force<3, false><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
-    else k_force<2, false><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);
+    if (nl) { if (gen) JDEM_FORCE(2, true, true); else JDEM_FORCE(2, true, false); }
+    else { if (gen) JDEM_FORCE(2, false, true); else JDEM_FORCE(2, false, false); }
   }
+#undef JDEM_FORCE
 }
 
 void launch_rot(int dim, const Bufs& b, const int32_t* sys_of, float4* q, float* angv, float* torque,

@@ -301,3 +301,33 @@ def test_verlet_list_paths_agree(nl):
             eng.close()
     assert min_image_diff(outs[1]["pos_c"], outs[0]["pos_c"], w.box_size) <= 1e-5
     assert force_err(outs[1]["force"], outs[0]["force"]) <= 1e-4
+
+
+def test_unwrapped_periodic_positions_match_wrapped():
+    """Periodic positions are never wrapped while stepping (domains/__init__.py:156-189):
+    particles displaced by whole box lengths must see the same contacts and forces, and a
+    rollout from such positions must follow the oracle run from the same positions."""
+    w = small_periodic(N=4096, radii=(0.5, 0.7), phi=0.55, seed=31)
+    rng = np.random.default_rng(4)
+    shifted = (w.pos + rng.integers(-3, 4, size=w.pos.shape) * w.box_size).astype(F32)
+    sy = osystem(w)
+    st = ostate(w)
+    st.pos_c = shifted
+    ref, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    st.pos_c = w.pos.copy()
+    ref_wrapped, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    eng = make_engine(w, skin=0.2)
+    try:
+        eng.upload(pos=shifted, rad=w.rad, mass=w.mass, vel=w.vel)
+        eng.compute_force()
+        f0 = eng.download()["force"]
+        eng.step(40)
+        out = eng.download()
+    finally:
+        eng.close()
+    assert force_err(f0, ref) <= 1e-5
+    assert force_err(f0, ref_wrapped) <= 1e-5
+    pos, vel, frc = shifted.copy(), w.vel.copy(), np.zeros_like(shifted)
+    oracle.c_step(3, pos, vel, frc, w.rad, w.mass, domain="periodic", box=w.box_size, anchor=w.anchor,
+                  dt=w.dt, steps=40, cell_size=2 * float(w.rad.max()), acc64=True)
+    assert min_image_diff(out["pos_c"], pos, w.box_size) <= 1e-4
