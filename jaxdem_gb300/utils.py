@@ -71,3 +71,30 @@ def get_pair_forces_and_ids(state, system, cutoff=None, max_neighbors=None):
     delta = np.maximum(F32(0), R - r) * (i_ids != sj).astype(F32)
     f = ((k * delta * inv)[:, None] * rij).astype(F32) * valid[:, None]
     return state, system, np.column_stack((i_ids, j_ids)), f.astype(F32)
+
+
+def grid_state(*, n_per_axis, spacing, radius: float = 1.0, mass: float = 1.0, jitter: float = 0.0,
+               vel_range=None, radius_range=None, mass_range=None, seed: int = 0):
+    """Particles on a rectangular lattice (``utils/grid_state.py:21-130``).
+
+    Same lattice (``meshgrid(indexing="ij")`` of ``arange(n) * spacing``) and
+    the same uniform ranges; random draws come from numpy's PCG64 instead of
+    JAX's PRNG, so the values differ from the reference's for equal seeds.
+    """
+    from .state import State
+
+    n_per_axis = tuple(int(n) for n in n_per_axis)
+    dim = len(n_per_axis)
+    sp = (float(spacing),) * dim if np.isscalar(spacing) else tuple(float(s) for s in spacing)
+    axes = [np.arange(n) * s for n, s in zip(n_per_axis, sp)]
+    coords = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).reshape(-1, dim).astype(F32)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    N = coords.shape[0]
+    if jitter > 0:
+        coords = (coords + rng.uniform(-jitter, jitter, coords.shape)).astype(F32)
+    rad = (rng.uniform(radius_range[0], radius_range[1], N) if radius_range is not None
+           else np.full(N, radius)).astype(F32)
+    m = (rng.uniform(mass_range[0], mass_range[1], N) if mass_range is not None else np.full(N, mass)).astype(F32)
+    vr = (-1.0, 1.0) if vel_range is None else tuple(vel_range)
+    vel = rng.uniform(vr[0], vr[1], coords.shape).astype(F32)
+    return State.create(pos=coords, vel=vel, rad=rad, mass=m)

@@ -720,12 +720,22 @@ def step(st: OState, sy: OSystem, n: int, **kw):
 # ---------------------------------------------------------------------------
 
 
-def compute_energy(st: OState, sy: OSystem):
+def naive_energy(st: OState, sy: OSystem) -> float:
+    """Collider PE over all pairs (``colliders/naive.py``; pair term x0.5, ``_partition.py:39-51``)."""
+    N = st.N
+    ii, jj = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    e = spring_energy_pair(ii, jj, st.pos_c, st.rad, st.mat_id, sy.young_eff, sy)
+    ok = valid_mask(st.clump_id[ii], st.clump_id[jj], st.bond_id[ii], jj, sy.interact_same_bond_id)
+    return float(np.sum(np.where(ok, st.pos_c.dtype.type(0.5) * e, 0).astype(np.float64)))
+
+
+def compute_energy(st: OState, sy: OSystem, naive: bool = False):
     """``thermal.compute_energy`` (``utils/thermal.py:153-177``), accumulated in float64.
 
     Returns ``(pe_pair, pe_gravity, ke_trans, ke_rot)``.
     """
-    pe_pair = cell_list_energy(st, sy, sum_dtype=np.float64)
+    pe_pair = naive_energy(st, sy) if naive else cell_list_energy(st, sy, sum_dtype=np.float64)
     g = sy.gravity.astype(np.float64)
     pe_grav = -float(np.sum((st.pos_c.astype(np.float64) @ g) * st.mass.astype(np.float64)))
     ke_t = float(np.sum(0.5 * st.mass.astype(np.float64) * np.sum(st.vel.astype(np.float64) ** 2, axis=1)))

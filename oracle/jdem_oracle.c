@@ -21,10 +21,50 @@
  *   direct Euler           jaxdem/integrators/direct_euler.py:30-66
  * Spheres only (clump_id = iota, pos_p = 0, no bonds).  Cell coordinates are
  * clamped into the grid (see dem_ref.cell_coords).  Built with
- * -ffp-contract=off so every float operation rounds as written.
+ * -ffp-contract=off so every floating-point operation rounds as written.
  */
 #include <math.h>
 #include <stdint.h>
+/* One source, two builds: float (default, the engine's arithmetic) and, with
+ * -DJDEM_ORACLE_F64, double (the reference's jax_enable_x64 tests). */
+/* Round half to even (jnp.round) without a libm call: adding and subtracting
+ * 1.5 * 2^(mantissa bits) rounds in the default mode; exact for |x| below
+ * 2^(mantissa bits - 1), otherwise rint. */
+static inline float rint_f(float x) {
+  const float m = 12582912.0f; /* 1.5 * 2^23 */
+  if (x < 4194304.0f && x > -4194304.0f) {
+    volatile float t = x + m;
+    return t - m;
+  }
+  return rintf(x);
+}
+static inline double rint_d(double x) {
+  const double m = 6755399441055744.0; /* 1.5 * 2^52 */
+  if (x < 2251799813685248.0 && x > -2251799813685248.0) {
+    volatile double t = x + m;
+    return t - m;
+  }
+  return rint(x);
+}
+#ifdef JDEM_ORACLE_F64
+typedef double real;
+#define FN(name) name##_f64
+#define R_SQRT sqrt
+#define R_FLOOR floor
+#define R_CEIL ceil
+#define R_RINT rint_d
+#define R_FMOD fmod
+#define R_FABS fabs
+#else
+typedef float real;
+#define FN(name) name
+#define R_SQRT sqrtf
+#define R_FLOOR floorf
+#define R_CEIL ceilf
+#define R_RINT rint_f
+#define R_FMOD fmodf
+#define R_FABS fabsf
+#endif
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -36,25 +76,25 @@ enum { LIN_NONE = 0, LIN_VERLET = 1, LIN_EULER = 2 };
 
 typedef struct {
   int dim, domain;
-  float box[3], anchor[3], inv_box[3];
-  float cell_req; /* requested cell size (collider.cell_size) */
+  real box[3], anchor[3], inv_box[3];
+  real cell_req; /* requested cell size (collider.cell_size) */
   int sr;         /* search range */
   int64_t g[3], stride[3];
-  float cell[3];
+  real cell[3];
   int64_t ncell;
   int n_mat;
-  const float* young;
+  const real* young;
 } Grid;
 
 static void grid_setup(Grid* G) {
   for (int a = 0; a < G->dim; ++a) {
     if (G->domain == DOM_PERIODIC) {
-      int64_t g = (int64_t)floorf(G->box[a] / G->cell_req);
+      int64_t g = (int64_t)R_FLOOR(G->box[a] / G->cell_req);
       if (g < 1) g = 1;
       G->g[a] = g;
-      G->cell[a] = G->box[a] / (float)g;
+      G->cell[a] = G->box[a] / (real)g;
     } else {
-      int64_t g = (int64_t)ceilf(G->box[a] / G->cell_req);
+      int64_t g = (int64_t)R_CEIL(G->box[a] / G->cell_req);
       if (g < 1) g = 1;
       G->g[a] = g;
       G->cell[a] = G->cell_req;
@@ -65,20 +105,20 @@ static void grid_setup(Grid* G) {
   G->ncell = G->stride[G->dim - 1] * G->g[G->dim - 1];
 }
 
-static inline float floor_mod1(float x) {
-  float m = fmodf(x, 1.0f);
+static inline real floor_mod1(real x) {
+  real m = R_FMOD(x, 1.0f);
   if (m < 0.0f) m = m + 1.0f;
   return m;
 }
 
-static inline void coords_of(const Grid* G, const float* p, int64_t* c) {
+static inline void coords_of(const Grid* G, const real* p, int64_t* c) {
   for (int a = 0; a < G->dim; ++a) {
-    float v;
+    real v;
     if (G->domain == DOM_PERIODIC) {
-      float frac = floor_mod1((p[a] - G->anchor[a]) / G->box[a]);
-      v = floorf(frac * (float)G->g[a]);
+      real frac = floor_mod1((p[a] - G->anchor[a]) / G->box[a]);
+      v = R_FLOOR(frac * (real)G->g[a]);
     } else {
-      v = floorf((p[a] - G->anchor[a]) / G->cell_req);
+      v = R_FLOOR((p[a] - G->anchor[a]) / G->cell_req);
     }
     int64_t ci = (int64_t)v;
     if (ci < 0) ci = 0;
@@ -89,7 +129,7 @@ static inline void coords_of(const Grid* G, const float* p, int64_t* c) {
 
 /* Stable counting sort of particles by cell hash: perm lists particle
  * indices cell by cell, ascending index within a cell (lax.sort is stable). */
-static void build_cells(const Grid* G, int64_t n, const float* pos, int64_t* hash, int64_t* start,
+static void build_cells(const Grid* G, int64_t n, const real* pos, int64_t* hash, int64_t* start,
                         int64_t* perm) {
   int d = G->dim;
 #pragma omp parallel for schedule(static)
@@ -110,31 +150,31 @@ static void build_cells(const Grid* G, int64_t n, const float* pos, int64_t* has
 }
 
 /* Force on i due to j: spring.py:97-108 with periodic._displacement. */
-static inline void spring_pair(const Grid* G, const float* pi, const float* pj, float ri, float rj,
-                               float k, int same, float* f) {
+static inline void spring_pair(const Grid* G, const real* pi, const real* pj, real ri, real rj,
+                               real k, int same, real* f) {
   int d = G->dim;
-  float rij[3];
-  float R = ri + rj;
+  real rij[3];
+  real R = ri + rj;
   for (int a = 0; a < d; ++a) {
-    float x = pi[a] - pj[a];
-    if (G->domain == DOM_PERIODIC) x = x - G->box[a] * rintf(x * G->inv_box[a]);
+    real x = pi[a] - pj[a];
+    if (G->domain == DOM_PERIODIC) x = x - G->box[a] * R_RINT(x * G->inv_box[a]);
     rij[a] = x;
   }
-  float d_sq = rij[0] * rij[0];
+  real d_sq = rij[0] * rij[0];
   for (int a = 1; a < d; ++a) d_sq = d_sq + rij[a] * rij[a];
-  float inv = (d_sq == 0.0f) ? 0.0f : 1.0f / sqrtf(d_sq > 1e-16f ? d_sq : 1e-16f);
-  float r = d_sq * inv;
-  float delta = R - r;
+  real inv = (d_sq == 0.0f) ? 0.0f : 1.0f / R_SQRT(d_sq > 1e-16f ? d_sq : 1e-16f);
+  real r = d_sq * inv;
+  real delta = R - r;
   if (!(delta > 0.0f)) delta = 0.0f;
   delta = delta * (same ? 0.0f : 1.0f);
-  float mag = k * delta * inv;
+  real mag = k * delta * inv;
   for (int a = 0; a < d; ++a) f[a] = mag * rij[a];
 }
 
 /* compute_force via the cell list in the reference's visiting order. */
-static void cell_list_force(const Grid* G, int64_t n, const float* pos, const float* rad,
+static void cell_list_force(const Grid* G, int64_t n, const real* pos, const real* rad,
                             const int32_t* mat, const int64_t* hash, const int64_t* start,
-                            const int64_t* perm, float* force, int acc64) {
+                            const int64_t* perm, real* force, int acc64) {
   int d = G->dim;
   int side = 2 * G->sr + 1;
   int M = d == 3 ? side * side * side : side * side;
@@ -164,8 +204,11 @@ static void cell_list_force(const Grid* G, int64_t n, const float* pos, const fl
       }
       nh[m] = oob ? -1 : h;
     }
-    if (G->domain == DOM_PERIODIC) {
-      /* _dedup_stencil_hashes: an entry equal to an earlier one becomes -1 */
+    int small_grid = 0;
+    for (int a = 0; a < d; ++a) small_grid |= G->g[a] < side;
+    if (G->domain == DOM_PERIODIC && small_grid) {
+      /* _dedup_stencil_hashes: an entry equal to an earlier one becomes -1
+       * (duplicates exist only when some axis has fewer than 2*sr+1 cells) */
       int64_t orig[343];
       memcpy(orig, nh, sizeof(int64_t) * (size_t)M);
       for (int b = 0; b < M; ++b)
@@ -176,19 +219,19 @@ static void cell_list_force(const Grid* G, int64_t n, const float* pos, const fl
           }
     }
     double tot64[3] = {0, 0, 0};
-    float tot[3] = {0, 0, 0};
+    real tot[3] = {0, 0, 0};
     for (int m = 0; m < M; ++m) {
       int64_t h = nh[m];
       if (h < 0) continue;
-      float acc[3] = {0, 0, 0};
+      real acc[3] = {0, 0, 0};
       double acc64v[3] = {0, 0, 0};
       int64_t k0 = start[h], k1 = start[h + 1];
       for (int64_t k = k0; k < k1; k += 4) {
-        float chunk[3] = {0, 0, 0};
+        real chunk[3] = {0, 0, 0};
         for (int u = 0; u < 4 && k + u < k1; ++u) {
           int64_t j = perm[k + u];
-          float f[3];
-          float kk = G->young[mat[i] * G->n_mat + mat[j]];
+          real f[3];
+          real kk = G->young[mat[i] * G->n_mat + mat[j]];
           spring_pair(G, pos + i * d, pos + j * d, rad[i], rad[j], kk, i == j, f);
           for (int a = 0; a < d; ++a) {
             chunk[a] = chunk[a] + f[a];
@@ -202,28 +245,28 @@ static void cell_list_force(const Grid* G, int64_t n, const float* pos, const fl
         tot64[a] += acc64v[a];
       }
     }
-    for (int a = 0; a < d; ++a) force[i * d + a] = acc64 ? (float)tot64[a] : tot[a];
+    for (int a = 0; a < d; ++a) force[i * d + a] = acc64 ? (real)tot64[a] : tot[a];
   }
   (void)hash;
 }
 
 /* _toc.verlet_collision_fraction for one coordinate. */
-static inline float toc_alpha(float v_end, float acc, float delta, float ws, float dt) {
-  float v_0 = v_end - dt * acc;
-  float v_mid = v_end - 0.5f * dt * acc;
-  float v_0_n = v_0 * ws, v_mid_n = v_mid * ws, acc_n = acc * ws;
-  float A = 0.5f * acc_n * dt * dt;
-  float B = v_0_n * dt;
-  float dw = delta + v_mid_n * dt;
-  float disc = B * B + 4.0f * A * dw;
+static inline real toc_alpha(real v_end, real acc, real delta, real ws, real dt) {
+  real v_0 = v_end - dt * acc;
+  real v_mid = v_end - 0.5f * dt * acc;
+  real v_0_n = v_0 * ws, v_mid_n = v_mid * ws, acc_n = acc * ws;
+  real A = 0.5f * acc_n * dt * dt;
+  real B = v_0_n * dt;
+  real dw = delta + v_mid_n * dt;
+  real disc = B * B + 4.0f * A * dw;
   if (!(disc > 0.0f)) disc = 0.0f;
-  float sq = disc > 0.0f ? sqrtf(disc) : 0.0f;
-  float alpha;
+  real sq = disc > 0.0f ? R_SQRT(disc) : 0.0f;
+  real alpha;
   if (B < 0.0f) {
-    float den = (B - sq < -1e-10f) ? B - sq : -1.0f;
+    real den = (B - sq < -1e-10f) ? B - sq : -1.0f;
     alpha = 2.0f * dw / den;
   } else {
-    float den = (fabsf(2.0f * A) > 1e-10f) ? 2.0f * A : 1.0f;
+    real den = (R_FABS(2.0f * A) > 1e-10f) ? 2.0f * A : 1.0f;
     alpha = (-B - sq) / den;
   }
   if (alpha < 0.0f) alpha = 0.0f;
@@ -232,40 +275,40 @@ static inline float toc_alpha(float v_end, float acc, float delta, float ws, flo
 }
 
 /* ReflectDomain.apply for one sphere (segment reductions are identities). */
-static inline void reflect_one(int d, const float* box, const float* anchor, float e, float dt,
-                               float* p, float* v, const float* F, float rad, float mass,
+static inline void reflect_one(int d, const real* box, const real* anchor, real e, real dt,
+                               real* p, real* v, const real* F, real rad, real mass,
                                int fixed) {
-  float inv_mass = 1.0f / mass;
-  float denom = inv_mass + 0.0f;
+  real inv_mass = 1.0f / mass;
+  real denom = inv_mass + 0.0f;
   if (denom == 0.0f) denom = 1.0f;
-  float delta[3], ws[3], act[3], acc[3], alpha[3];
+  real delta[3], ws[3], act[3], acc[3], alpha[3];
   for (int a = 0; a < d; ++a) {
-    float lo = anchor[a] + rad, hi = anchor[a] + box[a] - rad;
-    float olo = lo - p[a];
+    real lo = anchor[a] + rad, hi = anchor[a] + box[a] - rad;
+    real olo = lo - p[a];
     if (!(olo > 0.0f)) olo = 0.0f;
-    float ohi = p[a] - hi;
+    real ohi = p[a] - hi;
     if (!(ohi > 0.0f)) ohi = 0.0f;
     delta[a] = olo > ohi ? olo : ohi;
     ws[a] = (olo > 0.0f ? 1.0f : 0.0f) - (ohi > 0.0f ? 1.0f : 0.0f);
-    act[a] = fabsf(ws[a]);
+    act[a] = R_FABS(ws[a]);
     acc[a] = F[a] * inv_mass;
     alpha[a] = toc_alpha(v[a], acc[a], delta[a], ws[a], dt);
   }
-  float amin = 1.0f;
+  real amin = 1.0f;
   for (int a = 0; a < d; ++a) {
-    float x = act[a] > 0.0f ? alpha[a] : 1.0f;
+    real x = act[a] > 0.0f ? alpha[a] : 1.0f;
     if (x < amin) amin = x;
   }
-  float dt_factor = (amin - 1.0f) * dt;
-  float dt_rem = (1.0f - amin) * dt;
+  real dt_factor = (amin - 1.0f) * dt;
+  real dt_rem = (1.0f - amin) * dt;
   for (int a = 0; a < d; ++a) {
-    float vc = v[a] + dt_factor * acc[a];
-    float j = -(1.0f + e) * vc / denom;
-    float closing = (vc * ws[a]) < 0.0f ? 1.0f : 0.0f;
-    float cs = act[a] > 1.0f ? act[a] : 1.0f;
-    float w = act[a] / cs;
+    real vc = v[a] + dt_factor * acc[a];
+    real j = -(1.0f + e) * vc / denom;
+    real closing = (vc * ws[a]) < 0.0f ? 1.0f : 0.0f;
+    real cs = act[a] > 1.0f ? act[a] : 1.0f;
+    real w = act[a] / cs;
     j = j * (w * closing);
-    float dv = j * inv_mass;
+    real dv = j * inv_mass;
     if (fixed) dv = 0.0f;
     v[a] = v[a] + dv;
     p[a] = p[a] + dv * dt_rem;
@@ -275,12 +318,12 @@ static inline void reflect_one(int d, const float* box, const float* anchor, flo
 static int64_t max_i64(int64_t a, int64_t b) { return a > b ? a : b; }
 
 /* n steps of _step_once for spheres.  Returns 0 on success. */
-int oracle_step(int dim, int64_t n, int domain, const float* box_in, const float* anchor_in,
-                float restitution, const float* gravity, float dt, float cell_size,
-                int search_range, int n_mat, const float* young_eff, int linear, float* pos,
-                float* vel, float* force, const float* rad, const float* mass,
+int FN(oracle_step)(int dim, int64_t n, int domain, const real* box_in, const real* anchor_in,
+                real restitution, const real* gravity, real dt, real cell_size,
+                int search_range, int n_mat, const real* young_eff, int linear, real* pos,
+                real* vel, real* force, const real* rad, const real* mass,
                 const int32_t* mat_id, const uint8_t* fixed, int64_t steps, int n_threads,
-                int acc64, float* box_out, float* anchor_out) {
+                int acc64, real* box_out, real* anchor_out) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #endif
@@ -310,9 +353,9 @@ int oracle_step(int dim, int64_t n, int domain, const float* box_in, const float
                     force + i * dim, rad[i], mass[i], fixed[i]);
     } else if (domain == DOM_FREE && n > 0) {
       for (int a = 0; a < dim; ++a) {
-        float lo = pos[a] - rad[0], hi = pos[a] + rad[0];
+        real lo = pos[a] - rad[0], hi = pos[a] + rad[0];
         for (int64_t i = 1; i < n; ++i) {
-          float l = pos[i * dim + a] - rad[i], h = pos[i * dim + a] + rad[i];
+          real l = pos[i * dim + a] - rad[i], h = pos[i * dim + a] + rad[i];
           if (l < lo) lo = l;
           if (h > hi) hi = h;
         }
@@ -326,8 +369,8 @@ int oracle_step(int dim, int64_t n, int domain, const float* box_in, const float
     if (linear == LIN_VERLET) {
 #pragma omp parallel for schedule(static)
       for (int64_t i = 0; i < n; ++i) {
-        float sc = dt * 0.5f / mass[i];
-        float fr = fixed[i] ? 0.0f : 1.0f;
+        real sc = dt * 0.5f / mass[i];
+        real fr = fixed[i] ? 0.0f : 1.0f;
         for (int a = 0; a < dim; ++a) {
           vel[i * dim + a] = vel[i * dim + a] + force[i * dim + a] * sc * fr;
           pos[i * dim + a] = pos[i * dim + a] + dt * vel[i * dim + a];
@@ -346,16 +389,16 @@ int oracle_step(int dim, int64_t n, int domain, const float* box_in, const float
     /* 8. force_manager.apply (gravity), 9. linear after */
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-      float fr = fixed[i] ? 0.0f : 1.0f;
+      real fr = fixed[i] ? 0.0f : 1.0f;
       for (int a = 0; a < dim; ++a) {
-        float fcom = gravity[a] * (mass[i] / 1.0f);
-        float f = force[i * dim + a] + 0.0f + fcom;
+        real fcom = gravity[a] * (mass[i] / 1.0f);
+        real f = force[i * dim + a] + 0.0f + fcom;
         force[i * dim + a] = f;
         if (linear == LIN_VERLET) {
-          float sc = dt * 0.5f / mass[i];
+          real sc = dt * 0.5f / mass[i];
           vel[i * dim + a] = vel[i * dim + a] + f * sc * fr;
         } else if (linear == LIN_EULER) {
-          float sc = dt / mass[i];
+          real sc = dt / mass[i];
           vel[i * dim + a] = vel[i * dim + a] + f * sc * fr;
           pos[i * dim + a] = pos[i * dim + a] + dt * vel[i * dim + a];
         }
@@ -373,9 +416,9 @@ int oracle_step(int dim, int64_t n, int domain, const float* box_in, const float
 }
 
 /* collider.compute_force alone (no integration): forces at the given positions. */
-int oracle_force(int dim, int64_t n, int domain, const float* box, const float* anchor,
-                 float cell_size, int search_range, int n_mat, const float* young_eff,
-                 const float* pos, const float* rad, const int32_t* mat_id, float* force,
+int FN(oracle_force)(int dim, int64_t n, int domain, const real* box, const real* anchor,
+                 real cell_size, int search_range, int n_mat, const real* young_eff,
+                 const real* pos, const real* rad, const int32_t* mat_id, real* force,
                  int n_threads, int acc64) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
@@ -405,7 +448,7 @@ int oracle_force(int dim, int64_t n, int domain, const float* box, const float* 
   return 0;
 }
 
-int oracle_max_threads(void) {
+int FN(oracle_max_threads)(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
 #else

@@ -1,0 +1,124 @@
+"""Host-side mirror of the JaxDEM API: registry, State/System construction, and the
+unsupported-configuration errors (all raised before any device call)."""
+
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+import pytest
+
+import jaxdem_gb300 as jdem
+from jaxdem_gb300.factory import _normalize_key
+
+F32 = np.float32
+
+
+def test_key_normalization():
+    """factory.py:28-35 / tests/test_public_api.py:24-36."""
+    for k in ("CellList", "cell_list", "cell-list", "Cell List", "celllist"):
+        assert _normalize_key(k) == "celllist"
+        assert type(jdem.Collider.create(k, state=jdem.State.create(pos=np.zeros((2, 3))))).__name__ == "DynamicCellList"
+
+
+def test_unknown_key_and_unknown_kwargs():
+    with pytest.raises(KeyError):
+        jdem.Collider.create("no_such_collider")
+    st = jdem.State.create(pos=np.zeros((2, 3)))
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        jdem.Collider.create("CellList", state=st, bogus=3)  # factory.py:479-492: dropped, warned
+        assert any("ignoring unknown keyword" in str(x.message) for x in w)
+    with pytest.raises(TypeError):  # Domain.Create forwards **kw to the constructor
+        jdem.Domain.create("periodic", dim=2, box_size=[1.0, 1.0], bogus=3)
+
+
+def test_duplicate_registration_rejected():
+    class Other(jdem.Collider):
+        pass
+
+    with pytest.raises(ValueError):
+        jdem.Collider.register("CellList")(Other)
+
+
+def test_state_create_defaults():
+    """state.py:640-862: mass from the material table, inertia 0.4 m r^2, relabelled clumps."""
+    mats = [jdem.Material.create("elastic", young=1e3, poisson=0.3, density=2.0)]
+    table = jdem.MaterialTable.from_materials(mats)
+    st = jdem.State.create(pos=np.zeros((3, 3)), rad=[0.5, 1.0, 0.5], mat_table=table)
+    vol = 4.0 / 3.0 * np.pi * np.array([0.125, 1.0, 0.125])
+    assert np.allclose(st.mass, 2.0 * vol, rtol=1e-6)
+    assert np.allclose(st.inertia[:, 0], 0.4 * st.mass * st.rad ** 2, rtol=1e-6)
+    assert st.q.w.shape == (3, 1) and np.all(st.q.w == 1)
+    assert np.array_equal(st.clump_id, [0, 1, 2])
+    st2 = jdem.State.create(pos=np.zeros((3, 2)), clump_id=[7, 7, 3])
+    assert np.array_equal(st2.clump_id, [1, 1, 0])
+    assert st2.ang_vel.shape == (3, 1)
+
+
+def test_bond_table_is_symmetrised():
+    """state.py:735-761: bonds given one way become symmetric, -1 padded."""
+    st = jdem.State.create(pos=np.zeros((3, 2)), bond_id=[[1], [2], [-1]])
+    rows = [set(r[r >= 0].tolist()) for r in st.bond_id]
+    assert rows == [{1}, {0, 2}, {1}]
+
+
+def test_harmonic_and_linear_matchers():
+    mats = [jdem.Material.create("elastic", young=1e3, poisson=0.3),
+            jdem.Material.create("elastic", young=3e3, poisson=0.3)]
+    h = jdem.MaterialTable.from_materials(mats)
+    lin = jdem.MaterialTable.from_materials(mats, matcher=jdem.MaterialMatchmaker.create("linear"))
+    assert np.isclose(h.young_eff[0, 1], 2 * 1e3 * 3e3 / 4e3)
+    assert np.isclose(lin.young_eff[0, 1], 2e3)
+
+
+def test_system_create_components_and_validation():
+    st = jdem.State.create(pos=np.random.default_rng(0).uniform(0, 5, (20, 3)), rad=np.full(20, 0.5))
+    sy = jdem.System.create(state=st, collider_type="CellList", domain_type="periodic",
+                            domain_kw=dict(box_size=[5, 5, 5]), dt=1e-3)
+    assert sy.collider.type_name == "celllist" and np.isclose(sy.collider.cell_size, 1.0)
+    assert sy.collider.neighbor_mask.shape == (27, 3)
+    assert sy.domain.periodic and np.allclose(sy.domain.inv_box_size, 0.2)
+    with pytest.raises(ValueError):
+        jdem.System.create(state_shape=(4, 3), state=st)
+    with pytest.raises(TypeError):
+        jdem.System.create()
+    with pytest.raises(ValueError):
+        jdem.System.create(state=st, domain_type="periodic", domain_kw=dict(box_size=[5, 5]))
+    with pytest.raises(ValueError):
+        jdem.System.create(state=st, domain_type="reflect", domain_kw=dict(box_size=[5, 5, 5],
+                                                                            restitution_coefficient=1.5))
+
+
+def test_unsupported_configurations_raise_before_device_work():
+    from jaxdem_gb300 import session
+
+    st = jdem.State.create(pos=np.zeros((4, 3)), clump_id=[0, 0, 1, 1])
+    sy = jdem.System.create(state=st, collider_type="CellList")
+    with pytest.raises(NotImplementedError):
+        session.engine_for(st, sy)
+    st2 = jdem.State.create(pos=np.zeros((4, 3)))
+    fm = jdem.ForceManager.create((4, 3), force_functions=[lambda p, s, y: (p, p)])
+    sy2 = jdem.System.create(state=st2, collider_type="CellList", force_manager=fm)
+    with pytest.raises(NotImplementedError):
+        session.engine_for(st2, sy2)
+    sy3 = jdem.System.create(state=st2, collider_type="CellList",
+                             user_pre_step_actions=lambda s, y: (s, y))
+    with pytest.raises(NotImplementedError):
+        session.engine_for(st2, sy3)
+
+
+def test_trajectory_rollout_argument_checks():
+    st = jdem.State.create(pos=np.zeros((2, 3)))
+    sy = jdem.System.create(state=st)
+    with pytest.raises(ValueError):
+        jdem.System.trajectory_rollout(st, sy)
+    with pytest.raises(ValueError):
+        jdem.System.trajectory_rollout(st, sy, strides=np.ones((2, 2), int))
+
+
+def test_grid_state_lattice():
+    st = jdem.utils.grid_state(n_per_axis=(2, 3), spacing=1.5, radius=0.4, seed=1)
+    assert st.pos_c.shape == (6, 2)
+    assert np.allclose(sorted(set(st.pos_c[:, 1].tolist())), [0.0, 1.5, 3.0])
+    assert np.all((st.vel >= -1) & (st.vel <= 1))

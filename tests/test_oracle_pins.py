@@ -1,0 +1,257 @@
+"""Pin the oracle (CPU restatement) against the reference's own known answers.
+
+JaxDEM cannot run here (no JAX), and it ships no golden arrays; these tests
+restate the reference tests that pin the hot path, plus hand-derived
+analytic cases, on the numpy and C restatements:
+
+* ``tests/test_excluded_pairs.py:11-61``: bonded pairs are masked, F1 = 0, F0 = -F2;
+* ``tests/test_colliders_invariance.py:365-402``: the cell list equals the all-pairs sum;
+* ``tests/test_energy_conservation.py:34-107``: Verlet energy-error slope > 1.8,
+  Euler > 0.7, spheres in periodic / reflect / free domains, 2D and 3D;
+* ``tests/test_rotation_integrators.py:24-97``: torque-driven asymmetric body
+  against the closed form, relative error < 1e-4;
+* two overlapping spheres (|F| = k delta), a periodic image pair, a wall bounce.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from jaxdem_gb300 import workloads as W
+from oracle import dem_ref as R
+
+F32 = np.float32
+
+
+def _sys(dim, domain="periodic", box=None, anchor=None, rad=None, young=1e3, dt=1e-3, gravity=None,
+         linear="verlet", rotation="", dtype=F32):
+    cell, mask = R.cell_list_create(rad, dim, dtype=dtype)
+    box = np.full(dim, 10.0, dtype) if box is None else np.asarray(box, dtype)
+    anchor = np.zeros(dim, dtype) if anchor is None else np.asarray(anchor, dtype)
+    return R.OSystem(dim=dim, domain=domain, box_size=box, anchor=anchor,
+                     young_eff=np.array([[young]], dtype), dt=dtype(dt), cell_size=cell, neighbor_mask=mask,
+                     gravity=np.zeros(dim, dtype) if gravity is None else np.asarray(gravity, dtype),
+                     linear=linear, rotation=rotation)
+
+
+def test_excluded_pairs():
+    """tests/test_excluded_pairs.py:11-61 on the restatement (cell list and all pairs)."""
+    pos = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]], F32)
+    rad = np.full(3, 1.1, F32)
+    bond = np.array([[1, -1], [0, 2], [1, -1]])
+    st = R.make_state(pos, rad=rad, bond_id=bond)
+    # linear matcher of one material: young_eff = young = 1000
+    sy = _sys(2, domain="free", box=[1, 1], rad=rad)
+    for f in (R.cell_list_force(st, sy)[0], R.naive_force(st, sy)):
+        assert np.allclose(f[1], 0.0, atol=1e-5)
+        assert abs(f[0, 0]) > 0.1 and abs(f[2, 0]) > 0.1
+        assert np.allclose(f[0], -f[2], atol=1e-5)
+
+
+def test_two_sphere_spring_analytic():
+    """F = k delta r_hat (spring.py:97-108), E = k delta^2 / 2 per pair."""
+    k, r0, r1, d = 1e3, 0.5, 0.7, 1.0
+    pos = np.array([[1.0, 2.0, 3.0], [1.0 + d, 2.0, 3.0]], F32)
+    rad = np.array([r0, r1], F32)
+    st = R.make_state(pos, rad=rad)
+    sy = _sys(3, domain="free", rad=rad, young=k)
+    f, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    delta = r0 + r1 - d
+    assert np.allclose(f[0], [-k * delta, 0, 0], rtol=1e-6)
+    assert np.allclose(f[1], [k * delta, 0, 0], rtol=1e-6)
+    assert np.isclose(R.cell_list_energy(st, sy), 0.5 * k * delta ** 2, rtol=1e-6)
+
+
+def test_periodic_image_pair():
+    """Minimum image across the boundary (periodic.py:74-79)."""
+    L = 10.0
+    pos = np.array([[0.2, 5.0, 5.0], [9.6, 5.0, 5.0]], F32)
+    rad = np.full(2, 0.5, F32)
+    st = R.make_state(pos, rad=rad)
+    sy = _sys(3, domain="periodic", box=[L, L, L], rad=rad)
+    f, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    delta = 1.0 - 0.6
+    assert np.allclose(f[0], [1e3 * delta, 0, 0], rtol=1e-5)
+    assert np.allclose(f[1], [-1e3 * delta, 0, 0], rtol=1e-5)
+    pairs = R.contact_pairs(st, sy)
+    assert pairs.tolist() == [[0, 1]]
+
+
+def test_reflect_wall_bounce_analytic():
+    """Free flight into a wall (reflect.py:99-299, _toc.py:11-94): with F = 0 the collision
+    fraction is 1 - delta / (|v| dt); the velocity flips and the overshoot is mirrored."""
+    v, dt = -2.0, 1e-3
+    x0 = 0.5 + 0.0015  # distance to the wall contact point = 1.5e-3 < |v| dt = 2e-3
+    pos = np.array([[x0, 5.0]], F32)
+    vel = np.array([[v, 0.0]], F32)
+    st = R.make_state(pos, vel=vel, rad=np.array([0.5], F32))
+    sy = _sys(2, domain="reflect", box=[10, 10], rad=st.rad, dt=dt)
+    st, sy = R.step(st, sy, 1)  # drift overshoots the wall by 5e-4
+    st = R.reflect_apply(st, sy)  # next step's apply
+    assert np.isclose(st.vel[0, 0], -v, rtol=1e-5)
+    assert np.isclose(st.pos_c[0, 0], 0.5 + 5e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("domain", ["periodic", "reflect", "free"])
+@pytest.mark.parametrize("poly", [1.0, 2.0, 3.0])
+def test_cell_list_equals_all_pairs(dim, domain, poly):
+    """tests/test_colliders_invariance.py:365-402: the cell list sums the same pairs."""
+    rng = np.random.default_rng(100 + dim)
+    N = 300 if dim == 3 else 200
+    rad = rng.uniform(0.5 / poly, 0.5, N).astype(F32)
+    L = 7.0 if dim == 3 else 11.0
+    pos = rng.uniform(0, L, (N, dim)).astype(F32)
+    st = R.make_state(pos, rad=rad)
+    sy = _sys(dim, domain=domain, box=np.full(dim, L), rad=rad)
+    a, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    b = R.naive_force(st, sy, sum_dtype=np.float64)
+    assert np.allclose(a, b, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("domain", ["periodic", "reflect", "free"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_c_restatement_matches_numpy_bitwise(domain, dim):
+    """The C/OpenMP oracle steps bit-identically to the numpy oracle (float32)."""
+    w = W.c1(N=512, seed=5) if dim == 3 else W.c3(N=512, seed=5)
+    w.domain = domain
+    if domain == "reflect" and dim == 3:
+        w.pos = np.clip(w.pos, w.rad[:, None], w.box_size - w.rad[:, None]).astype(F32)
+    st = R.make_state(w.pos, vel=w.vel, rad=w.rad, mass=w.mass)
+    sy = _sys(dim, domain=domain, box=w.box_size, rad=w.rad, dt=w.dt, gravity=w.gravity)
+    st1, sy1 = R.step(st.copy(), sy, 5)
+    pos, vel, frc = w.pos.copy(), w.vel.copy(), np.zeros_like(w.pos)
+    box, anc = oracle.c_step(dim, pos, vel, frc, w.rad, w.mass, domain=domain, box=w.box_size,
+                             anchor=w.anchor, dt=w.dt, steps=5, cell_size=float(sy.cell_size),
+                             gravity=w.gravity, threads=2)
+    assert np.array_equal(pos, st1.pos_c)
+    assert np.array_equal(vel, st1.vel)
+    assert np.array_equal(frc, st1.force)
+    if domain == "free":
+        assert np.array_equal(box, sy1.box_size) and np.array_equal(anc, sy1.anchor)
+
+
+def _lattice(dim, poly, seed=42):
+    """set_up_spheres (tests/test_colliders_invariance.py:50-110): 64 spheres on a
+    1.2-spaced lattice, radii U[0.5/poly, 0.5], velocities U[-1, 1], mass 1, k = 1e3."""
+    n = int(round(64 ** (1 / dim)))
+    axes = [np.arange(n) * 1.2] * dim
+    pos = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, dim).astype(np.float64)
+    rng = np.random.default_rng(seed)
+    rad = rng.uniform(0.5 / poly, 0.5, len(pos))
+    vel = rng.uniform(-1, 1, pos.shape)
+    return pos, vel, rad, np.full(dim, 1.2 * n), np.full(dim, -0.5)
+
+
+def _energy_std(dim, domain, linear, dt, total=5.0, n_samples=100, dtype=np.float64):
+    """Std of the total energy over a run (the reference runs this under jax_enable_x64)."""
+    pos, vel, rad, box, anchor = _lattice(dim, 1.0)
+    pos, vel, rad = pos.astype(dtype), vel.astype(dtype), rad.astype(dtype)
+    box, anchor = box.astype(dtype), anchor.astype(dtype)
+    mass = np.ones(len(pos), dtype)
+    frc = np.zeros_like(pos)
+    steps = int(total / dt)
+    stride = max(1, steps // n_samples)
+    cell = 2 * float(rad.max())
+    es = []
+    st_e = R.make_state(pos, rad=rad, mass=mass, dtype=dtype)
+    sy_e = _sys(dim, domain=domain, box=box, anchor=anchor, rad=rad, dtype=dtype)
+    for _ in range(n_samples):
+        b2, a2 = oracle.c_step(dim, pos, vel, frc, rad, mass, domain=domain, box=box, anchor=anchor, dt=dt,
+                               steps=stride, cell_size=cell, linear=linear, threads=1, acc64=True)
+        st_e.pos_c, st_e.vel = pos.copy(), vel.copy()
+        if domain == "free":
+            sy_e.box_size, sy_e.anchor = b2, a2
+            sy_e.inv_box_size = (1 / b2).astype(dtype)
+        e = R.compute_energy(st_e, sy_e, naive=True)
+        es.append(e[0] + e[1] + e[2] + e[3])
+    return float(np.std(es))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("domain", ["periodic", "reflect", "free"])
+@pytest.mark.parametrize("linear", ["verlet", "euler"])
+def test_energy_conservation_order(dim, domain, linear):
+    """tests/test_energy_conservation.py:34-88: slope of log std(E) vs log dt."""
+    dts = np.logspace(np.log10(2e-3), np.log10(3e-5), 5)
+    stds = [_energy_std(dim, domain, linear, float(dt)) for dt in dts]
+    slope, _ = np.polyfit(np.log(dts), np.log(stds), 1)
+    if linear == "verlet":
+        assert slope > 1.8, (slope, stds)
+    else:
+        assert slope > 0.7, (slope, stds)
+
+
+@pytest.mark.parametrize("rot", ["spiral", "verletspiral"])
+def test_aspherical_rotation_closed_form(rot):
+    """tests/test_rotation_integrators.py:24-97 on the restated integrators (float64):
+    constant body-frame torque on an asymmetric body, 70,000 steps of 1e-5."""
+    rho, Rad, H = 7750.0, 0.05, 0.15
+    M = rho * np.pi * Rad * Rad * H
+    Ix = 0.5 * M * Rad * Rad
+    Iy = M * H * H / 12.0 + 0.25 * M * Rad * Rad
+    Iz = Iy
+    tx = Rad * 0.5
+    w0 = np.array([0.3, -0.9, 0.6])
+    f64 = np.float64
+    st = R.make_state(np.zeros((1, 3)), ang_vel=w0[None], mass=np.array([M]), rad=np.array([Rad]), dtype=f64)
+    st.inertia = np.array([[Ix, Iy, Iz]], f64)
+    sy = _sys(3, domain="free", rad=st.rad, dt=1e-5, rotation=rot, dtype=f64)
+    tb = np.array([[tx, 0.0, 0.0]])
+    torque_lab = lambda q: R.quat_rotate(q, tb)  # noqa: E731
+    st.torque = torque_lab(st.q)
+    for _ in range(70000):
+        if rot == "verletspiral":
+            st = R.vvspiral_before(st, sy)
+        st.torque = torque_lab(st.q)  # ForceManager: user torque in the lab frame
+        if rot == "verletspiral":
+            st = R.vvspiral_after(st, sy)
+        else:
+            st = R.spiral_after(st, sy)
+    t = 0.7
+    A = (Ix - Iy) * (Iz - Ix) / (Iy * Iz)
+    B = Iy / (Iz - Ix)
+    E = 2.0 * tx * B / Ix
+    wx = w0[0] + tx * t / Ix
+    eta = 0.5 * Ix * np.sqrt(-A) / tx
+    C = E * eta
+    K1 = (C * w0[1] * np.cos(eta * w0[0] ** 2) - w0[2] * np.sin(eta * w0[0] ** 2)) / C
+    K2 = (C * w0[1] * np.sin(eta * w0[0] ** 2) + w0[2] * np.cos(eta * w0[0] ** 2)) / C
+    D = eta * wx ** 2
+    ww = np.array([wx, K1 * np.cos(D) + K2 * np.sin(D), C * (K2 * np.cos(D) - K1 * np.sin(D))])
+    wb = R.quat_rotate_back(st.q, st.ang_vel)[0]
+    assert np.log10(np.linalg.norm(wb - ww) / np.linalg.norm(ww)) < -4.0
+
+
+@pytest.mark.parametrize("cfg,cell,grid", [("c1", 1.0, (17, 17, 17)), ("c2", 1.4, (87, 87, 87)),
+                                           ("c3", 1.2, (1820, 1820))])
+def test_grid_parameters_of_the_configurations(cfg, cell, grid):
+    """DynamicCellList.Create + _grid_params (cell_list.py:374-432, _partition.py:54-99)."""
+    w = {"c1": lambda: W.c1(), "c2": lambda: W.c2(N=4096), "c3": lambda: W.c3(N=4096)}[cfg]()
+    if cfg == "c2":  # box of the full-size system
+        w.box_size = np.full(3, 123.17252, F32)
+    if cfg == "c3":
+        w.box_size = np.full(2, 2183.75, F32)
+    c, mask = R.cell_list_create(w.rad if cfg != "c3" else np.array([0.4, 0.6], F32), w.dim)
+    assert np.isclose(c, cell, rtol=1e-6)
+    assert mask.shape == (3 ** w.dim, w.dim)
+    g, strides, _, ovf = R.grid_params(w.box_size, c, w.domain == "periodic")
+    assert tuple(g) == grid and not ovf
+
+
+def test_neighbor_list_properties():
+    """create_neighbor_list rows: within the cutoff, symmetric, no self, -1 padded."""
+    w = W.c1(N=600, seed=9)
+    st = R.make_state(w.pos, rad=w.rad)
+    sy = _sys(3, domain="periodic", box=w.box_size, rad=w.rad)
+    nl, ovf = R.create_neighbor_list(st, sy, 1.5, 40)
+    assert not ovf
+    rows = [set(r[r >= 0].tolist()) for r in nl]
+    for i, r in enumerate(rows):
+        assert i not in r
+        for j in r:
+            assert i in rows[j]
+            d = R.displacement_true(w.pos[i], w.pos[j], sy)
+            assert float(np.sum(d.astype(np.float64) ** 2)) <= 1.5 ** 2 * (1 + 1e-6)
