@@ -47,7 +47,10 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    p.add_argument("--no-batched", action="store_true", help="skip the batched mixed-size summary")
+    p.add_argument("--no-tune", action="store_true", help="skip the skin autotuner")
+    p.add_argument("--plain-sample", type=int, default=192, help="systems timed one at a time (batched baseline)")
     p.add_argument("--skin", type=float, default=None)
     p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -200,9 +203,24 @@ def run_ours(args, rank, world, dist):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
+    from jaxdem_gb300 import autotune
+
     w = make_workload(args.workload, args.n, rank)
-    skin = args.skin if args.skin is not None else 0.1 * float(w.rad.max())
     young = np.array([[W.K_SPRING]], np.float32)
+    rmax = float(w.rad.max())
+    tuning = None
+    if args.skin is not None:
+        skin = args.skin
+    elif args.no_tune:
+        skin = autotune.default_skin(rmax)
+    else:
+        def mk(sk):
+            return Engine(w.dim, [w.desc()], young, skin=sk, chunk_steps=CHUNK, device=dev)
+
+        skin, timings = autotune.tune_skin(mk, lambda e: e.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel),
+                                           rmax, key=autotune.workload_key(w))
+        tuning = {"skin_over_rmax": round(skin / rmax, 3),
+                  "ms_per_step_by_skin": {str(k): round(v * 1e3, 4) for k, v in timings.items()}}
     eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
     eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
@@ -288,7 +306,7 @@ def run_ours(args, rank, world, dist):
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": describe(w), "N": w.N, "skin": skin, "chunk_steps": CHUNK,
+        "config": {"workload": describe(w), "N": w.N, "skin": skin, "autotune": tuning, "chunk_steps": CHUNK,
                    "l2": "flushed (256 MB write) between timed 50-step chunks",
                    "parallelism": "replicas" if world > 1 else "single",
                    "resorts_in_timed_region": rebuilds_timed},
@@ -302,8 +320,62 @@ def run_ours(args, rank, world, dist):
         "clocks": clk,
     }
     eng.close()
+    if rank == 0 and world == 1 and not args.no_batched:
+        line["batched"] = run_batched(args, dev, flush, torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_batched(args, dev, flush, torch, n_systems=4096, steps=1000):
+    """Mixed-size batch: 4096 periodic 3D systems, N ~ logU[64, 16384], phi ~ U[0.3, 0.6],
+    1000 steps in 50-step graph chunks, against the plain kernel looped per system."""
+    from jaxdem_gb300 import workloads as W
+    from jaxdem_gb300._lib import Engine
+    from jaxdem_gb300.batch import BatchedSystems
+
+    ws = W.c4(n_systems=n_systems)
+    total = sum(w.N for w in ws)
+    rmax = max(float(w.rad.max()) for w in ws)
+    skin = args.skin if args.skin is not None else 0.65 * rmax
+    bs = BatchedSystems(ws, skin=skin, chunk_steps=CHUNK, device=dev)
+    bs.upload()
+    bs.step(CHUNK)  # warm-up: capture, first re-sort
+    stream = torch.cuda.ExternalStream(bs.engine.stream(), device=dev)
+    ms = 0.0
+    for _ in range(steps // CHUNK):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        bs.step_async(CHUNK)
+        b.record(stream)
+        b.synchronize()
+        ms += a.elapsed_time(b)
+    bs.engine.sync()
+    batched = total * steps / (ms * 1e-3)
+    bs.close()
+    # plain fused kernel looped per system: every k-th system, one handle each
+    k = max(1, n_systems // max(1, args.plain_sample))
+    sample = ws[::k]
+    p_steps = 100
+    t_sum, ps_sum = 0.0, 0
+    for w in sample:
+        e = Engine(3, [w.desc()], np.array([[W.K_SPRING]], np.float32), skin=skin, chunk_steps=CHUNK, device=dev)
+        e.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+        e.step(CHUNK)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.step(p_steps)
+        t_sum += time.perf_counter() - t0
+        ps_sum += w.N * p_steps
+        e.close()
+    plain = ps_sum / t_sum
+    return {"workload": f"{n_systems} periodic 3D systems, N~logU[64,16384] (total {total}), phi~U[0.3,0.6], "
+                        f"r 0.5/0.7, dt=1e-3, {steps} steps in {CHUNK}-step graph chunks",
+            "value": batched, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+            "plain_looped": plain, "batched_over_plain": batched / plain,
+            "plain_sample": f"{len(sample)} of {n_systems} systems stepped one at a time ({p_steps} steps each, "
+                            f"one handle and graph per system), throughput = sum(N*steps)/sum(time)"}
 
 
 def main():

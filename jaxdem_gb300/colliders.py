@@ -83,7 +83,9 @@ class DynamicCellList(Collider):
         mesh = np.meshgrid(*([r] * state.dim), indexing="ij")
         mask = np.stack([m.ravel() for m in mesh], axis=1).astype(np.int32)
         if skin is None:
-            skin = F32(0.1) * max_rad
+            from .autotune import default_skin
+
+            skin = default_skin(float(max_rad))
         return cls(neighbor_mask=mask, cell_size=F32(cell_size), skin=F32(skin))
 
     @property

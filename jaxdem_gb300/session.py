@@ -102,9 +102,11 @@ def _bond_width(state: State) -> int:
 
 
 def _skin(state: State, system) -> float:
+    from .autotune import default_skin
+
     s = getattr(system.collider, "skin", None)
     if s is None:
-        s = F32(0.1) * (F32(np.max(state.rad)) if state.rad.size else F32(1.0))
+        s = default_skin(float(np.max(state.rad)) if state.rad.size else 1.0)
     return float(s)
 
 
@@ -176,8 +178,9 @@ def download(eng: Engine, state: State) -> State:
     return st
 
 
-def _advance_system(system, eng: Engine, n: int, batched: bool):
-    """time += dt per step in float32 (system.py:62-66); free-domain frame from the device."""
+def _advance_system(system, eng: Engine, n: int, batched: bool, index: int = 0):
+    """time += dt per step in float32 (system.py:62-66); free-domain frame from the device
+    (all systems of the handle when ``batched``, else system ``index``)."""
     dt = np.asarray(system.dt, F32)
     t = np.asarray(system.time, F32).copy()
     for _ in range(n):
@@ -187,7 +190,7 @@ def _advance_system(system, eng: Engine, n: int, batched: bool):
     if dom.type_name == "free" and n > 0:
         box, anc = eng.domain_state()
         if not batched:
-            box, anc = box[0], anc[0]
+            box, anc = box[index], anc[index]
         dom = dataclasses.replace(dom, box_size=box.astype(F32), anchor=anc.astype(F32),
                                   inv_box_size=(F32(1.0) / box).astype(F32))
     return dataclasses.replace(system, time=t if t.ndim else F32(t), step_count=sc, domain=dom)
