@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the batched mixed-size summary")
     p.add_argument("--no-tune", action="store_true", help="skip the skin autotuner")
     p.add_argument("--plain-sample", type=int, default=192, help="systems timed one at a time (batched baseline)")
+    p.add_argument("--graph-mode", type=int, default=0, choices=[0, 1, 2],
+                   help="0 conditional re-sort nodes, 1 plain graphs (profilers see every kernel), 2 no graphs")
     p.add_argument("--skin", type=float, default=None)
     p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -177,7 +179,7 @@ def run_reference(args, rank, world):
 # -------------------------------------------------------------- ours
 def traffic_from_profile(workload):
     """dram bytes per fused-kernel launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"
+    p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"  # written from an ncu capture
     if p.exists():
         try:
             d = json.loads(p.read_text())
@@ -221,7 +223,7 @@ def run_ours(args, rank, world, dist):
                                            rmax, key=autotune.workload_key(w))
         tuning = {"skin_over_rmax": round(skin / rmax, 3),
                   "ms_per_step_by_skin": {str(k): round(v * 1e3, 4) for k, v in timings.items()}}
-    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
+    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev, graph_mode=args.graph_mode)
     eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -307,6 +309,7 @@ def run_ours(args, rank, world, dist):
         "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": describe(w), "N": w.N, "skin": skin, "autotune": tuning, "chunk_steps": CHUNK,
+                   "graph_mode": ["conditional re-sort nodes", "plain graphs", "direct launches"][args.graph_mode],
                    "l2": "flushed (256 MB write) between timed 50-step chunks",
                    "parallelism": "replicas" if world > 1 else "single",
                    "resorts_in_timed_region": rebuilds_timed},

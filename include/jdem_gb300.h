@@ -86,6 +86,10 @@ typedef struct {
   int32_t device;               /* CUDA device ordinal */
   int32_t neighbor_list;        /* Verlet list built at each re-sort: 0 = on (capacity from the
                                    density), > 0 = on with this initial capacity, -1 = off */
+  int32_t graph_mode;           /* 0: CUDA graphs whose re-sort kernels sit in conditional nodes;
+                                   1: plain graphs (re-sort kernels always launched, returning
+                                   early when no re-sort is due; profilers can see every node);
+                                   2: no graphs (direct launches) */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

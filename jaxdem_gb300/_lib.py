@@ -72,6 +72,7 @@ class Config(C.Structure):
         ("chunk_steps", C.c_int32),
         ("device", C.c_int32),
         ("neighbor_list", C.c_int32),
+        ("graph_mode", C.c_int32),
     ]
 
 
@@ -173,7 +174,7 @@ class Engine:
 
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
-                 device: int = 0, neighbor_list=True):
+                 device: int = 0, neighbor_list=True, graph_mode: int = 0):
         self.lib = load()
         self.dim = int(dim)
         self.n_per_system = [int(s["n"]) for s in systems]
@@ -216,6 +217,7 @@ class Engine:
         # an int > 0: list with that initial capacity
         cfg.neighbor_list = (-1 if neighbor_list is False else
                              (0 if neighbor_list is True else int(neighbor_list)))
+        cfg.graph_mode = int(graph_mode)
         self._descs = descs
         h = C.c_void_p()
         rc = self.lib.jdem_create(C.byref(cfg), C.byref(h))

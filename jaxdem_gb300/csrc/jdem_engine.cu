@@ -150,6 +150,9 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   bond_w = cfg->bond_width;
   interact_same_bond = cfg->interact_same_bond_id;
   use_nl = cfg->neighbor_list >= 0;
+  if (cfg->graph_mode < 0 || cfg->graph_mode > 2) return fail(JDEM_ERR_BAD_ARG, "config: graph_mode in 0..2");
+  graph_mode = cfg->graph_mode;
+  use_conditional = graph_mode == 0;
   nl_request = cfg->neighbor_list;
   desc.assign(cfg->systems, cfg->systems + S);
   P = 0;
@@ -514,6 +517,11 @@ int JdemHandle::capture_step_conditional(int mode, cudaGraphConditionalHandle hc
 }
 
 int JdemHandle::run_graph(long long nsteps, int mode_last) {
+  if (graph_mode == 2) {
+    for (long long k = 0; k < nsteps; ++k) enqueue_step(k + 1 == nsteps ? mode_last : MODE_STEP);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+    return JDEM_OK;
+  }
   // key: (nsteps, mode of the final step)
   long long key = nsteps * 64 + mode_last;
   auto it = graphs.find(key);

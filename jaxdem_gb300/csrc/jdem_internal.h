@@ -44,6 +44,7 @@ struct JdemHandle {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;     // captures the conditional re-sort bodies
   bool use_conditional = true;
+  int graph_mode = 0;
   bool own_stream = false;
   void* h_status = nullptr;
   std::map<long long, cudaGraphExec_t> graphs;
