@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     p.add_argument("--no-batched", action="store_true", help="skip the batched mixed-size summary")
+    p.add_argument("--no-served", action="store_true", help="skip the serving summary")
+    p.add_argument("--serve-requests", type=int, default=120, help="prefix of the request stream served")
+    p.add_argument("--serve-baseline", type=int, default=16, help="requests served one at a time (baseline)")
     p.add_argument("--no-tune", action="store_true", help="skip the skin autotuner")
     p.add_argument("--plain-sample", type=int, default=192, help="systems timed one at a time (batched baseline)")
     p.add_argument("--graph-mode", type=int, default=0, choices=[0, 1, 2],
@@ -325,6 +328,8 @@ def run_ours(args, rank, world, dist):
     eng.close()
     if rank == 0 and world == 1 and not args.no_batched:
         line["batched"] = run_batched(args, dev, flush, torch)
+    if rank == 0 and world == 1 and not args.no_served:
+        line["served"] = run_served(args, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -379,6 +384,29 @@ def run_batched(args, dev, flush, torch, n_systems=4096, steps=1000):
             "plain_looped": plain, "batched_over_plain": batched / plain,
             "plain_sample": f"{len(sample)} of {n_systems} systems stepped one at a time ({p_steps} steps each, "
                             f"one handle and graph per system), throughput = sum(N*steps)/sum(time)"}
+
+
+def run_served(args, dev):
+    """Continuous batching of the rollout-request stream (Poisson arrivals at 200/s,
+    N ~ logU[256, 262144], dim 2 or 3, phi ~ U[0.3, 0.6], steps ~ U{100..10000}):
+    a bounded prefix of the stream, against the plain kernel serving one at a time."""
+    from jaxdem_gb300 import serve
+    from jaxdem_gb300 import workloads as W
+
+    reqs = W.c5()
+    head = reqs[: args.serve_requests]
+    offered = sum(r.N * r.steps for r in head) / max(head[-1].arrival, 1e-9)
+    res = serve.run_stream(head, device=dev)
+    base = serve.run_one_at_a_time(reqs[: args.serve_baseline], device=dev)
+    return {"workload": f"first {len(head)} of 20000 requests (Poisson 200/s; N~logU[256,262144]; dim 2|3; "
+                        f"phi~U[0.3,0.6]; r~U[0.4,0.6]; steps~U{{100..10000}}), periodic, 150 GB HBM budget",
+            "value": res["throughput"], "unit": "particle-steps/s",
+            "latency_s": res["latency_s"], "queue_wait_s": res["queue_wait_s"], "completed": res["completed"],
+            "offered_load": offered, "makespan_s": res["makespan_s"],
+            "server_stats": res["server_stats"],
+            "one_at_a_time": {"requests": base["completed"], "throughput": base["throughput"],
+                              "busy_throughput": base["busy_throughput"], "latency_s": base["latency_s"]},
+            "served_over_one_at_a_time": res["throughput"] / base["busy_throughput"]}
 
 
 def main():

@@ -208,6 +208,67 @@ int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain, const flo
                                const float* anchor, float young, const float* pos, const float* rad,
                                float* force, void* stream);
 
+/* ---- Serving: continuous batching of rollout requests on one GPU ----------
+ * A request is one independent system (State + System) and a step count, the
+ * unit of System.step(state, system, n) / trajectory_rollout.  Requests are
+ * admitted in arrival order while the active set stays under max_active,
+ * target_particles and hbm_budget_bytes; every epoch advances all active
+ * requests together (one batched launch per kernel) by
+ * min(chunk_steps, smallest remaining count).  Between epochs a request's
+ * state stays on the device (repacked device-to-device when the active set
+ * changes).  Spheres only, one material; rotation integrators are not run. */
+typedef struct JdemServer JdemServer;
+
+typedef struct {
+  int32_t dim;               /* 2 or 3 (one server per dimension) */
+  int32_t device;
+  int32_t max_active;        /* concurrent requests (<= 0: 1024) */
+  int32_t chunk_steps;       /* steps per epoch at most (<= 0: 50) */
+  int64_t target_particles;  /* admit while the active particles stay below this (<= 0: 4 Mi) */
+  double hbm_budget_bytes;   /* admission limit on the resident footprint (<= 0: 150e9) */
+  float skin;                /* binning skin of the batch */
+  float young;               /* spring stiffness */
+} JdemServeConfig;
+
+typedef struct {
+  JdemSystemDesc system;     /* n, domain, integrators, dt, box, gravity */
+  int64_t steps;
+  const float* pos;          /* (n, dim) host arrays, copied at submit */
+  const float* vel;
+  const float* rad;
+  const float* mass;
+} JdemRequest;
+
+typedef struct {
+  int32_t state;             /* 0 pending, 1 active, 2 done, 3 cancelled, 4 failed */
+  int32_t status;            /* status code of a failed request */
+  int64_t n;
+  int64_t steps;             /* steps completed */
+  double submit_s, admit_s, done_s;  /* steady-clock seconds */
+} JdemRequestInfo;
+
+typedef struct {
+  int64_t submitted, completed, epochs, repacks, particle_steps, max_active, failures;
+  int64_t pending, active, bytes_in_use;
+} JdemServeStats;
+
+int jdem_serve_create(const JdemServeConfig* cfg, JdemServer** out);
+/* Thread-safe; validates and copies the request.  *id identifies it. */
+int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id);
+/* Cancel a pending or active request (takes effect at the next epoch). */
+int jdem_serve_cancel(JdemServer* s, int64_t id);
+/* Ids of requests that finished (done, cancelled or failed) since the last poll. */
+int jdem_serve_poll(JdemServer* s, int64_t* ids, int32_t cap, int32_t* count);
+/* Final pos_c, vel, force of a done request (any pointer may be NULL) and its timings. */
+int jdem_serve_result(JdemServer* s, int64_t id, float* pos, float* vel, float* force, JdemRequestInfo* info);
+/* Free a finished request's buffers. */
+int jdem_serve_release(JdemServer* s, int64_t id);
+/* Wait until no request is pending or active (timeout_s <= 0: no limit). */
+int jdem_serve_drain(JdemServer* s, double timeout_s);
+int jdem_serve_stats(JdemServer* s, JdemServeStats* out);
+const char* jdem_serve_last_error(JdemServer* s);
+int jdem_serve_destroy(JdemServer* s);
+
 /* Page-lock caller host memory for asynchronous copies (cudaHostRegister). */
 int jdem_host_register(void* ptr, size_t bytes);
 int jdem_host_unregister(void* ptr);

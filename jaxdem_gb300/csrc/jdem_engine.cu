@@ -154,74 +154,114 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   graph_mode = cfg->graph_mode;
   use_conditional = graph_mode == 0;
   nl_request = cfg->neighbor_list;
-  desc.assign(cfg->systems, cfg->systems + S);
-  P = 0;
-  for (int s = 0; s < S; ++s) {
-    const JdemSystemDesc& d = desc[s];
-    if (d.n < 0) return fail(JDEM_ERR_BAD_ARG, "system n < 0");
-    if (d.domain < 0 || d.domain > 2) return fail(JDEM_ERR_BAD_ARG, "unknown domain");
-    if (d.linear_integrator < 0 || d.linear_integrator > 2) return fail(JDEM_ERR_BAD_ARG, "unknown linear integrator");
-    if (d.rotation_integrator < 0 || d.rotation_integrator > 2)
-      return fail(JDEM_ERR_BAD_ARG, "unknown rotation integrator");
-    if (!(d.dt > 0.0f) && !(d.dt == 0.0f)) return fail(JDEM_ERR_BAD_ARG, "dt must be finite");
-    for (int a = 0; a < dim; ++a)
-      if (d.domain != DOM_FREE && !(d.box_size[a] > 0.0f))
-        return fail(JDEM_ERR_BAD_ARG, "box_size must be positive");
-    if (d.domain == DOM_REFLECT && !(d.restitution > 0.0f && d.restitution <= 1.0f))
-      return fail(JDEM_ERR_BAD_ARG, "restitution_coefficient must be in (0, 1]");
-    P += d.n;
-  }
-  if (P >= (1LL << 31) - 1) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "more than 2^31-2 particles");
+  int rc0 = set_systems(cfg->systems, S);
+  if (rc0) return rc0;
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   own_stream = true;
   JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, 64));
   int rc;
-  size_t p4 = sizeof(float4) * (size_t)std::max(P, 1LL);
-  size_t p1 = sizeof(int32_t) * (size_t)std::max(P, 1LL);
-  for (int k = 0; k < 2; ++k) {
-    if ((rc = dalloc((void**)&b.pos[k], p4))) return rc;
-    if ((rc = dalloc((void**)&b.vel[k], p4))) return rc;
-    if ((rc = dalloc((void**)&b.frc[k], p4))) return rc;
-    if ((rc = dalloc((void**)&b.tag[k], p1))) return rc;
-    if ((rc = dalloc((void**)&b.orig[k], p1))) return rc;
-    if ((rc = dalloc((void**)&b.key[k], p1))) return rc;
-  }
-  if ((rc = dalloc((void**)&b.key_tmp, p1))) return rc;
-  if ((rc = dalloc((void**)&b.slot_tmp, p1))) return rc;
-  if ((rc = dalloc((void**)&b.perm_tmp, p1))) return rc;
-  if ((rc = dalloc((void**)&b.sys, sizeof(SysParams) * S))) return rc;
   if ((rc = dalloc((void**)&b.ctl, sizeof(Ctl)))) return rc;
-  if ((rc = dalloc((void**)&b.bbox, sizeof(float) * 6 * S))) return rc;
   if ((rc = dalloc((void**)&d_young, sizeof(float) * n_mat * n_mat))) return rc;
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_young, cfg->young_eff, sizeof(float) * n_mat * n_mat,
                                       cudaMemcpyHostToDevice, stream));
-  if (bond_w > 0) {
-    if ((rc = dalloc((void**)&d_bond, sizeof(int32_t) * (size_t)std::max(P, 1LL) * bond_w))) return rc;
-  }
-  size_t pd = sizeof(float) * (size_t)std::max(P, 1LL) * dim;
-  int ad = dim == 3 ? 3 : 1;
-  size_t pa = sizeof(float) * (size_t)std::max(P, 1LL) * ad;
-  if ((rc = dalloc((void**)&st_pos, pd))) return rc;
-  if ((rc = dalloc((void**)&st_vel, pd))) return rc;
-  if ((rc = dalloc((void**)&st_frc, pd))) return rc;
-  if ((rc = dalloc((void**)&st_rad, p1))) return rc;
-  if ((rc = dalloc((void**)&st_mass, p1))) return rc;
-  if ((rc = dalloc((void**)&st_mat, p1))) return rc;
-  if ((rc = dalloc((void**)&st_fixed, (size_t)std::max(P, 1LL)))) return rc;
-  if ((rc = dalloc((void**)&st_sys, p1))) return rc;
-  if ((rc = dalloc((void**)&d_q, p4))) return rc;
-  if ((rc = dalloc((void**)&d_w, pa))) return rc;
-  if ((rc = dalloc((void**)&d_tq, pa))) return rc;
-  if ((rc = dalloc((void**)&d_inertia, pa))) return rc;
+  if ((rc = ensure_capacity(P, S))) return rc;
   b.young = d_young;
-  b.bond = d_bond;
-  b.P = P;
-  b.S = S;
   b.n_mat = n_mat;
   b.bond_w = bond_w;
   b.interact_same_bond = interact_same_bond;
-  // system index of every particle (caller order)
+  if ((rc = bind_systems())) return rc;
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  return JDEM_OK;
+}
+
+// Validate and adopt a system list (sets desc, S, P).
+int JdemHandle::set_systems(const JdemSystemDesc* systems, int n_systems) {
+  if (!systems || n_systems < 1) return fail(JDEM_ERR_BAD_ARG, "at least one system is required");
+  if ((uint32_t)n_systems > TAG_SYS_MASK) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "too many systems");
+  long long p = 0;
+  for (int s = 0; s < n_systems; ++s) {
+    const JdemSystemDesc& d = systems[s];
+    if (d.n < 0) return fail(JDEM_ERR_BAD_ARG, "system n < 0");
+    if (d.domain < 0 || d.domain > 2) return fail(JDEM_ERR_BAD_ARG, "unknown domain");
+    if (d.linear_integrator < 0 || d.linear_integrator > 2) return fail(JDEM_ERR_BAD_ARG, "unknown linear integrator");
+    if (d.rotation_integrator < 0 || d.rotation_integrator > 2)
+      return fail(JDEM_ERR_BAD_ARG, "unknown rotation integrator");
+    if (!std::isfinite(d.dt)) return fail(JDEM_ERR_BAD_ARG, "dt must be finite");
+    for (int a = 0; a < dim; ++a)
+      if (d.domain != DOM_FREE && !(d.box_size[a] > 0.0f)) return fail(JDEM_ERR_BAD_ARG, "box_size must be positive");
+    if (d.domain == DOM_REFLECT && !(d.restitution > 0.0f && d.restitution <= 1.0f))
+      return fail(JDEM_ERR_BAD_ARG, "restitution_coefficient must be in (0, 1]");
+    p += d.n;
+  }
+  if (p >= (1LL << 31) - 1) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "more than 2^31-2 particles");
+  desc.assign(systems, systems + n_systems);
+  S = n_systems;
+  P = p;
+  return JDEM_OK;
+}
+
+// Grow every particle- and system-sized array to hold p_need particles and
+// s_need systems (growth by 1.5x; shrinking keeps the allocation).
+int JdemHandle::ensure_capacity(long long p_need, int s_need) {
+  int rc;
+  if (p_need > p_cap || p_cap == 0) {
+    long long cap = std::max(std::max(p_need, 1LL), p_cap + p_cap / 2);
+    drop_graphs();
+    void** arrays[] = {(void**)&b.pos[0], (void**)&b.pos[1], (void**)&b.vel[0], (void**)&b.vel[1],
+                       (void**)&b.frc[0], (void**)&b.frc[1], (void**)&b.tag[0], (void**)&b.tag[1],
+                       (void**)&b.orig[0], (void**)&b.orig[1], (void**)&b.key[0], (void**)&b.key[1],
+                       (void**)&b.key_tmp, (void**)&b.slot_tmp, (void**)&b.perm_tmp, (void**)&st_pos,
+                       (void**)&st_vel, (void**)&st_frc, (void**)&st_rad, (void**)&st_mass, (void**)&st_mat,
+                       (void**)&st_fixed, (void**)&st_sys, (void**)&d_q, (void**)&d_w, (void**)&d_tq,
+                       (void**)&d_inertia, (void**)&d_bond, (void**)&b.nbr, (void**)&b.ncnt, (void**)&b.posw};
+    for (void** a : arrays) {
+      dfree(*a);
+      *a = nullptr;
+    }
+    b.nl_cap = 0;
+    nl_alloc_p = 0;
+    size_t p4 = sizeof(float4) * (size_t)cap, p1 = sizeof(int32_t) * (size_t)cap;
+    size_t pd = sizeof(float) * (size_t)cap * dim;
+    size_t pa = sizeof(float) * (size_t)cap * (dim == 3 ? 3 : 1);
+    for (int k = 0; k < 2; ++k) {
+      if ((rc = dalloc((void**)&b.pos[k], p4))) return rc;
+      if ((rc = dalloc((void**)&b.vel[k], p4))) return rc;
+      if ((rc = dalloc((void**)&b.frc[k], p4))) return rc;
+      if ((rc = dalloc((void**)&b.tag[k], p1))) return rc;
+      if ((rc = dalloc((void**)&b.orig[k], p1))) return rc;
+      if ((rc = dalloc((void**)&b.key[k], p1))) return rc;
+    }
+    if ((rc = dalloc((void**)&b.key_tmp, p1)) || (rc = dalloc((void**)&b.slot_tmp, p1)) ||
+        (rc = dalloc((void**)&b.perm_tmp, p1)) || (rc = dalloc((void**)&st_pos, pd)) ||
+        (rc = dalloc((void**)&st_vel, pd)) || (rc = dalloc((void**)&st_frc, pd)) ||
+        (rc = dalloc((void**)&st_rad, p1)) || (rc = dalloc((void**)&st_mass, p1)) ||
+        (rc = dalloc((void**)&st_mat, p1)) || (rc = dalloc((void**)&st_fixed, (size_t)cap)) ||
+        (rc = dalloc((void**)&st_sys, p1)) || (rc = dalloc((void**)&d_q, p4)) || (rc = dalloc((void**)&d_w, pa)) ||
+        (rc = dalloc((void**)&d_tq, pa)) || (rc = dalloc((void**)&d_inertia, pa)))
+      return rc;
+    if (bond_w > 0 && (rc = dalloc((void**)&d_bond, sizeof(int32_t) * (size_t)cap * bond_w))) return rc;
+    p_cap = cap;
+  }
+  if (s_need > s_cap) {
+    int cap = std::max(s_need, s_cap + s_cap / 2);
+    drop_graphs();
+    dfree(b.sys);
+    dfree(b.bbox);
+    b.sys = nullptr;
+    b.bbox = nullptr;
+    if ((rc = dalloc((void**)&b.sys, sizeof(SysParams) * cap)) || (rc = dalloc((void**)&b.bbox, sizeof(float) * 6 * cap)))
+      return rc;
+    s_cap = cap;
+  }
+  b.bond = d_bond;
+  return JDEM_OK;
+}
+
+// Per-particle system index (caller order) for the current system list.
+int JdemHandle::bind_systems() {
+  b.P = P;
+  b.S = S;
   std::vector<int32_t> sys_of((size_t)std::max(P, 1LL));
   long long off = 0;
   for (int s = 0; s < S; ++s)
@@ -232,8 +272,51 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   return JDEM_OK;
 }
 
-// Grid + cell arrays from the uploaded radii (host copy rad_h) and positions.
+// Replace the system list of a live handle (serving): capacity grows as
+// needed, graphs are dropped when the shape changes, and the new state must
+// be uploaded before stepping.
+int JdemHandle::rebind(const JdemSystemDesc* systems, int n_systems) {
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  int rc = set_systems(systems, n_systems);
+  if (rc) return rc;
+  if ((rc = ensure_capacity(P, S))) return rc;
+  drop_graphs();
+  uploaded = false;
+  return bind_systems();
+}
+
+// Grid + cell arrays from the uploaded radii (host copy rad_h) and positions:
+// per-system maximum radius and bounding box, then plan_grid.
 int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
+  std::vector<float> rmax((size_t)S, 0.0f), lo((size_t)S * 3, 0.0f), hi((size_t)S * 3, 1.0f);
+  long long off = 0;
+  for (int s = 0; s < S; ++s) {
+    const long long n = desc[s].n;
+    if (n > 0) {
+      for (int a = 0; a < dim; ++a) {
+        lo[(size_t)s * 3 + a] = 3.4e38f;
+        hi[(size_t)s * 3 + a] = -3.4e38f;
+      }
+      for (long long i = off; i < off + n; ++i) {
+        float r = rad_h[i];
+        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(JDEM_ERR_BAD_ARG, "radius must be finite and >= 0");
+        rmax[(size_t)s] = std::max(rmax[(size_t)s], r);
+        for (int a = 0; a < dim; ++a) {
+          float x = pos_h[i * dim + a];
+          if (!std::isfinite(x)) return fail(JDEM_ERR_NONFINITE, "non-finite position in upload");
+          lo[(size_t)s * 3 + a] = std::min(lo[(size_t)s * 3 + a], x - r);
+          hi[(size_t)s * 3 + a] = std::max(hi[(size_t)s * 3 + a], x + r);
+        }
+      }
+    }
+    off += n;
+  }
+  return plan_grid(rmax.data(), lo.data(), hi.data());
+}
+
+// Per-system grids from the maximum radius and (free domain) bounding box,
+// cell arrays sized to fit, then the Verlet-list capacity.
+int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* hi_s) {
   sys_h.assign((size_t)S, SysParams{});
   long long c_total = 0, off = 0;
   any_free = false;
@@ -255,34 +338,20 @@ int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
     sp.restitution = d.restitution;
     sp.p0 = off;
     sp.np = d.n;
-    float rmax = 0.0f;
     float lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
-    if (d.n > 0) {
-      for (int a = 0; a < dim; ++a) {
-        lo[a] = 3.4e38f;
-        hi[a] = -3.4e38f;
-      }
-      for (long long i = off; i < off + d.n; ++i) {
-        float r = rad_h[i];
-        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(JDEM_ERR_BAD_ARG, "radius must be finite and >= 0");
-        rmax = std::max(rmax, r);
-        for (int a = 0; a < dim; ++a) {
-          float x = pos_h[i * dim + a];
-          if (!std::isfinite(x)) return fail(JDEM_ERR_NONFINITE, "non-finite position in upload");
-          lo[a] = std::min(lo[a], x - r);
-          hi[a] = std::max(hi[a], x + r);
-        }
-      }
+    for (int a = 0; a < dim; ++a) {
+      lo[a] = lo_s[(size_t)s * 3 + a];
+      hi[a] = hi_s[(size_t)s * 3 + a];
     }
     if (d.domain == DOM_FREE) any_free = true;
-    choose_grid(sp, dim, rmax, skin, d.n, lo, hi);
+    choose_grid(sp, dim, rmax_s[s], skin, d.n, lo, hi);
     sp.c0 = c_total;
     c_total += sp.ncap;
     if (c_total >= (1LL << 31) - 2)
       return fail(JDEM_ERR_HASH_OVERFLOW, "total cell count exceeds the int32 hash range");
     off += d.n;
   }
-  if (c_total != C) {
+  if (c_total > c_cap) {
     drop_graphs();
     dfree(b.cell_start);
     dfree(b.cnt);
@@ -293,28 +362,27 @@ int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
     if ((rc = dalloc((void**)&b.cnt, sizeof(int32_t) * (size_t)c_total))) return rc;
     long long nb = (c_total + 2047) / 2048 + 1;
     if ((rc = dalloc((void**)&b.scan_blk, sizeof(int32_t) * (size_t)nb))) return rc;
-    C = c_total;
-    b.C = C;
+    c_cap = c_total;
   }
+  if (c_total != C) drop_graphs();
+  C = c_total;
+  b.C = C;
   JDEM_CUDA_TRY(this, cudaMemsetAsync(b.cnt, 0, sizeof(int32_t) * (size_t)C, stream));
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.sys, sys_h.data(), sizeof(SysParams) * S, cudaMemcpyHostToDevice, stream));
+  JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
   if (!use_nl) return plan_list(0);
   // Verlet-list capacity: expected neighbours within 2 r_max + skin at the
   // densest system, plus eight standard deviations of a Poisson count.
   double mean_max = 0.0;
-  off = 0;
   for (int s = 0; s < S; ++s) {
     const SysParams& sp = sys_h[s];
-    double vol = 1.0, rl = 0.0;
-    float rmax = 0.0f;
-    for (long long i = off; i < off + desc[s].n; ++i) rmax = std::max(rmax, rad_h[i]);
-    rl = 2.0 * rmax + skin;
+    double vol = 1.0;
+    double rl = 2.0 * rmax_s[s] + skin;
     for (int a = 0; a < dim; ++a)
       vol *= sp.domain == DOM_FREE ? std::max(1e-30, (double)sp.g[a] * (double)sp.gcell[a]) : (double)sp.box[a];
     double sphere = dim == 3 ? 4.18879 * rl * rl * rl : 3.14159 * rl * rl;
     double mean = desc[s].n / vol * sphere;
     mean_max = std::max(mean_max, mean);
-    off += desc[s].n;
   }
   int cap = (int)std::ceil(mean_max + 8.0 * std::sqrt(mean_max) + 16.0);
   cap = std::min(256, (cap + 7) / 8 * 8);
@@ -324,7 +392,7 @@ int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
 
 // (Re)allocate the Verlet list for cap entries per slot (0: no list).
 int JdemHandle::plan_list(int cap) {
-  if (cap == b.nl_cap && (cap == 0 || b.nbr)) return JDEM_OK;
+  if (cap == b.nl_cap && (cap == 0 || (b.nbr && P <= nl_alloc_p))) return JDEM_OK;
   drop_graphs();
   dfree(b.nbr);
   dfree(b.ncnt);
@@ -340,8 +408,11 @@ int JdemHandle::plan_list(int cap) {
   size_t slices = (size_t)((P + 31) / 32);
   if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)cap * 32 * slices))) return rc;
   if ((rc = dalloc((void**)&b.ncnt, sizeof(int32_t) * (size_t)P))) return rc;
-  if (!b.posw && (rc = dalloc((void**)&b.posw, sizeof(float4) * (size_t)P))) return rc;
+  dfree(b.posw);
+  b.posw = nullptr;
+  if ((rc = dalloc((void**)&b.posw, sizeof(float4) * (size_t)P))) return rc;
   b.nl_cap = cap;
+  nl_alloc_p = P;
   return JDEM_OK;
 }
 
@@ -459,6 +530,50 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
   sticky_status = 0;
   uploaded = true;
   JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  return JDEM_OK;
+}
+
+// Upload from device arrays already in the reference layout, without any
+// host read: per-system maximum radius and bounding box come from the caller.
+// Spheres only; materials, fixed flags and rotational state take their
+// defaults (material 0, free, identity orientation, zero spin).
+int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
+                                const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s) {
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  int rc = plan_grid(rmax_s, lo_s, hi_s);
+  if (rc) return rc;
+  size_t N = (size_t)P;
+  int ad = dim == 3 ? 3 : 1;
+  if (N) {
+    cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_pos, d_pos, N * dim * 4, k, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_vel, d_vel, N * dim * 4, k, stream));
+    if (d_frc) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_frc, d_frc, N * dim * 4, k, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_frc, 0, N * dim * 4, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_rad, d_rad, N * 4, k, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_mass, d_mass, N * 4, k, stream));
+    JDEM_CUDA_TRY(this, cudaMemsetAsync(st_mat, 0, N * 4, stream));
+    JDEM_CUDA_TRY(this, cudaMemsetAsync(st_fixed, 0, N, stream));
+    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
+    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
+    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_inertia, 0, N * ad * 4, stream));
+    launch_identity_q((float4*)d_q, (long long)N, stream);
+    rot_active = false;
+    launch_pack(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, st_mat, st_fixed, st_sys, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+  }
+  if ((rc = reset_ctl())) return rc;
+  cur_box.assign((size_t)S * 3, 0.0f);
+  cur_anchor.assign((size_t)S * 3, 0.0f);
+  for (int s2 = 0; s2 < S; ++s2)
+    for (int a = 0; a < 3; ++a) {
+      cur_box[(size_t)s2 * 3 + a] = a < dim ? desc[s2].box_size[a] : 0.0f;
+      cur_anchor[(size_t)s2 * 3 + a] = a < dim ? desc[s2].anchor[a] : 0.0f;
+    }
+  bbox_pending = false;
+  steps_done = 0;
+  sticky_status = 0;
+  uploaded = true;
   return JDEM_OK;
 }
 

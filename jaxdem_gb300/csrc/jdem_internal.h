@@ -14,6 +14,10 @@ struct JdemHandle {
   int S = 0;
   long long P = 0;
   long long C = 0;
+  long long p_cap = 0;  // allocated particle capacity
+  long long c_cap = 0;  // allocated cell capacity
+  int s_cap = 0;        // allocated system capacity
+  long long nl_alloc_p = 0;
   float skin = 0.0f;
   int chunk = 50;
   int n_mat = 1;
@@ -64,7 +68,14 @@ struct JdemHandle {
   void dfree(void* p);
   void drop_graphs();
   int setup(const JdemConfig* cfg);
+  int set_systems(const JdemSystemDesc* systems, int n_systems);
+  int ensure_capacity(long long p_need, int s_need);
+  int bind_systems();
+  int rebind(const JdemSystemDesc* systems, int n_systems);
   int plan_cells(const float* rad_h, const float* pos_h);
+  int plan_grid(const float* rmax_s, const float* lo_s, const float* hi_s);
+  int upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
+                      const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s);
   int plan_list(int cap);
   int reset_ctl();
   int upload(const JdemHostState* s, bool device_ptrs);

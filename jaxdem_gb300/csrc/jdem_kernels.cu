@@ -995,6 +995,38 @@ void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, con
   else k_pack<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc, rad, mass, mat, fixed, sys_of);
 }
 
+__global__ void k_identity_q(float4* q, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) q[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+}
+
+void launch_identity_q(float4* q, long long n, cudaStream_t st) {
+  if (n > 0) k_identity_q<<<nblk(n, 256), 256, 0, st>>>(q, n);
+}
+
+// Copy particle segments [src, src + n) -> [dst, dst + n) of `width` floats per
+// particle for several arrays at once (serving: repack resident requests).
+// seg[3k] = source particle offset, seg[3k + 1] = destination offset, seg[3k + 2] = count.
+__global__ void k_segcopy(const long long* __restrict__ seg, int nseg, int narr, const float* const* __restrict__ src,
+                          float* const* __restrict__ dst, const int* __restrict__ width) {
+  int k = blockIdx.y;
+  if (k >= nseg) return;
+  long long so = seg[3 * k], dof = seg[3 * k + 1], n = seg[3 * k + 2];
+  for (int a = 0; a < narr; ++a) {
+    int w = width[a];
+    long long tot = n * w;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x)
+      dst[a][dof * w + i] = src[a][so * w + i];
+  }
+}
+
+void launch_segcopy(const long long* seg, int nseg, int narr, const float* const* src, float* const* dst,
+                    const int* width, cudaStream_t st) {
+  if (nseg <= 0) return;
+  dim3 g(64, (unsigned int)nseg);
+  k_segcopy<<<g, 256, 0, st>>>(seg, nseg, narr, src, dst, width);
+}
+
 void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st) {
   if (b.P == 0) return;
   if (dim == 3) k_unpack<3><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc);

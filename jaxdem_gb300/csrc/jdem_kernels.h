@@ -8,6 +8,9 @@ void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, con
                  const float* rad, const float* mass, const int32_t* mat, const uint8_t* fixed,
                  const int32_t* sys_of, cudaStream_t st);
 void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st);
+void launch_identity_q(float4* q, long long n, cudaStream_t st);
+void launch_segcopy(const long long* seg, int nseg, int narr, const float* const* src, float* const* dst,
+                    const int* width, cudaStream_t st);
 void launch_scan(const Bufs& b, cudaStream_t st);
 void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
 int rebuild_kernel_count(bool any_free);

@@ -41,10 +41,12 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_binding_covers_the_header(lib):
+    from jaxdem_gb300 import serve
     from jaxdem_gb300._lib import EXPORTED
 
+    bound = set(EXPORTED) | {p[0] for p in serve._PROTOS}
     extra = {"jdem_compute_force_noalloc"}  # bound in its own test file
-    assert set(declared()) - extra <= set(EXPORTED)
+    assert set(declared()) - extra <= bound
 
 
 def test_abi_version_and_status_strings(lib):
@@ -69,3 +71,25 @@ def test_config_struct_layout_matches_header(lib):
     assert C.sizeof(SystemDesc) == 8 + 4 * 4 + 12 + 12 + 4 + 12 + 4 + 4
     assert C.sizeof(HostState) == 12 * C.sizeof(C.c_void_p)
     assert C.sizeof(Config) >= 4 * 2 + C.sizeof(C.c_void_p)
+
+
+def test_struct_sizes_match_the_c_header(tmp_path):
+    """Compile a probe against include/jdem_gb300.h and compare with the ctypes mirrors."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    from jaxdem_gb300 import serve
+    from jaxdem_gb300._lib import Config, HostState, Stats, SystemDesc
+
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include "jdem_gb300.h"\nint main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n",'
+                   "sizeof(JdemSystemDesc),sizeof(JdemConfig),sizeof(JdemHostState),sizeof(JdemStats),"
+                   "sizeof(JdemServeConfig),sizeof(JdemRequest),sizeof(JdemRequestInfo),sizeof(JdemServeStats));}")
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    want = [C.sizeof(t) for t in (SystemDesc, Config, HostState, Stats, serve.ServeConfig, serve.RequestStruct,
+                                  serve.RequestInfo, serve.ServeStats)]
+    assert got == want

@@ -1,0 +1,154 @@
+"""Serving loop: continuous batching, admission, cancellation, and the
+requirement that each request's result is the same alone and in the mix
+(tolerance: 1e-5 position, minimum image)."""
+
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import pytest
+
+from jaxdem_gb300 import workloads as W
+from jaxdem_gb300._lib import Engine, JdemError
+from jaxdem_gb300.autotune import default_skin
+from jaxdem_gb300.serve import Server
+from tests.helpers import min_image_diff
+
+pytestmark = pytest.mark.gpu
+
+F32 = np.float32
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build(built):
+    return built
+
+
+def req(N, seed, dim=3, phi=0.3, steps=200):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return W.periodic_system(f"r{seed}", rng, N, dim, rng.uniform(0.4, 0.6, N), phi, 0.05, 1e-3, steps)
+
+
+def engine_result(w):
+    eng = Engine(w.dim, [w.desc()], np.array([[W.K_SPRING]], F32), skin=default_skin(0.6))
+    try:
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+        eng.step(w.steps)
+        return eng.download()
+    finally:
+        eng.close()
+
+
+def test_alone_equals_in_mix():
+    a = req(1500, 1, steps=200)
+    s = Server(3)
+    try:
+        ia = s.submit(a)
+        s.drain(120)
+        alone = s.result(ia)
+    finally:
+        s.close()
+    mix = [req(500, 2, steps=50), a, req(3000, 3, phi=0.45, steps=120), req(256, 4, steps=400)]
+    s = Server(3)
+    try:
+        ids = [s.submit(w) for w in mix]
+        s.drain(120)
+        res = [s.result(i) for i in ids]
+        st = s.stats()
+    finally:
+        s.close()
+    assert st["max_active"] >= 2 and st["repacks"] >= 3
+    for w, r in zip(mix, res):
+        assert r["info"]["state"] == "done" and r["info"]["steps"] == w.steps
+    assert min_image_diff(res[1]["pos_c"], alone["pos_c"], a.box_size) <= 1e-5
+    ref = engine_result(a)
+    assert min_image_diff(alone["pos_c"], ref["pos_c"], a.box_size) <= 1e-5
+    for w, r in zip(mix, res):
+        assert min_image_diff(r["pos_c"], engine_result(w)["pos_c"], w.box_size) <= 1e-5
+
+
+def test_cancellation_leaves_others_untouched():
+    ws = [req(800, 10, dim=2, phi=0.5, steps=300), req(1200, 11, dim=2, phi=0.5, steps=300),
+          req(600, 12, dim=2, phi=0.5, steps=150)]
+    s = Server(2)
+    try:
+        ids = [s.submit(w) for w in ws]
+        s.cancel(ids[1])
+        s.drain(120)
+        infos = [s.info(i) for i in ids]
+        res = {i: s.result(i) for i, inf in zip(ids, infos) if inf["state"] == "done"}
+    finally:
+        s.close()
+    assert infos[1]["state"] == "cancelled"
+    for k in (0, 2):
+        assert infos[k]["state"] == "done"
+        assert min_image_diff(res[ids[k]]["pos_c"], engine_result(ws[k])["pos_c"], ws[k].box_size) <= 1e-5
+
+
+def test_hbm_budget_limits_concurrency():
+    ws = [req(1000, 20 + k, steps=60) for k in range(4)]
+    s = Server(3, hbm_budget_gb=0.0008)  # room for one 1000-particle request
+    try:
+        ids = [s.submit(w) for w in ws]
+        s.drain(120)
+        st = s.stats()
+        states = [s.info(i)["state"] for i in ids]
+        with pytest.raises(JdemError):
+            s.submit(req(5000, 30, steps=10))  # larger than the whole budget
+    finally:
+        s.close()
+    assert st["max_active"] == 1 and states == ["done"] * 4
+
+
+def test_bad_input_rejected_at_submit():
+    w = req(100, 40, steps=10)
+    w.pos[3, 1] = np.nan
+    s = Server(3)
+    try:
+        with pytest.raises(JdemError):
+            s.submit(w)
+        ok = s.submit(req(100, 41, steps=10))
+        s.drain(60)
+        assert s.info(ok)["state"] == "done"
+    finally:
+        s.close()
+
+
+def test_two_dimensions_served_concurrently():
+    w2, w3 = req(2000, 50, dim=2, phi=0.6, steps=150), req(2000, 51, dim=3, phi=0.4, steps=150)
+    s2, s3 = Server(2), Server(3)
+    try:
+        i2, i3 = s2.submit(w2), s3.submit(w3)
+        s2.drain(120)
+        s3.drain(120)
+        r2, r3 = s2.result(i2), s3.result(i3)
+    finally:
+        s2.close()
+        s3.close()
+    assert min_image_diff(r2["pos_c"], engine_result(w2)["pos_c"], w2.box_size) <= 1e-5
+    assert min_image_diff(r3["pos_c"], engine_result(w3)["pos_c"], w3.box_size) <= 1e-5
+
+
+def test_release_while_batch_continues():
+    """A finished request may be released while the rest of its batch still runs;
+    the server keeps serving the others with the same results."""
+    short, long_ = req(400, 60, steps=20), req(1500, 61, steps=300)
+    s = Server(3, chunk_steps=10)
+    try:
+        i_long, i_short = s.submit(long_), s.submit(short)
+        t0 = time.time()
+        while s.info(i_short)["state"] != "done" and time.time() - t0 < 60:
+            time.sleep(0.0005)
+        assert s.info(i_short)["state"] == "done"
+        s.result(i_short)
+        s.release(i_short)
+        with pytest.raises(JdemError):
+            s.release(i_short)  # unknown id after release
+        s.drain(120)
+        r = s.result(i_long)
+        st = s.stats()
+    finally:
+        s.close()
+    assert st["completed"] == 2 and st["active"] == 0 and st["pending"] == 0
+    assert min_image_diff(r["pos_c"], engine_result(long_)["pos_c"], long_.box_size) <= 1e-5
