@@ -315,7 +315,9 @@ def run_ours(args, rank, world, dist):
                    "graph_mode": ["conditional re-sort nodes", "plain graphs", "direct launches"][args.graph_mode],
                    "l2": "flushed (256 MB write) between timed 50-step chunks",
                    "parallelism": "replicas" if world > 1 else "single",
-                   "resorts_in_timed_region": rebuilds_timed},
+                   "resorts_in_timed_region": rebuilds_timed,
+                   "verlet_list": {"capacity": stats["list_capacity"], "tiles": stats["list_tiles"],
+                                   "regrowths": stats["list_regrowths"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_force (fused force + integrate)", "bytes_per_unit": B,

@@ -121,6 +121,9 @@ typedef struct {
   uint32_t device_status;    /* sticky device status bits */
   int32_t graphs;            /* instantiated CUDA graphs */
   int64_t device_bytes;      /* device memory held by the handle */
+  int64_t list_regrowths;    /* Verlet-list capacity doublings after a row overflowed */
+  int32_t list_capacity;     /* entries per Verlet-list row (0: no list) */
+  int32_t list_tiles;        /* cell bricks of the shared-memory list path (0: slot-order path) */
 } JdemStats;
 
 /* ABI version of the loaded library (JDEM_ABI_VERSION). */

@@ -104,6 +104,9 @@ class Stats(C.Structure):
         ("device_status", C.c_uint32),
         ("graphs", C.c_int32),
         ("device_bytes", C.c_int64),
+        ("list_regrowths", C.c_int64),
+        ("list_capacity", C.c_int32),
+        ("list_tiles", C.c_int32),
     ]
 
 

@@ -18,7 +18,7 @@ using namespace jdem;
 
 namespace {
 
-// largest Verlet-list row the list build can stage in shared memory
+// largest Verlet-list row
 constexpr int kMaxListCap = 384;
 
 const char* kStatusNames[] = {"ok",          "bad argument", "capacity overflow", "hash overflow",
@@ -214,13 +214,15 @@ int JdemHandle::ensure_capacity(long long p_need, int s_need) {
                        (void**)&b.key_tmp, (void**)&b.slot_tmp, (void**)&b.perm_tmp, (void**)&st_pos,
                        (void**)&st_vel, (void**)&st_frc, (void**)&st_rad, (void**)&st_mass, (void**)&st_mat,
                        (void**)&st_fixed, (void**)&st_sys, (void**)&d_q, (void**)&d_w, (void**)&d_tq,
-                       (void**)&d_inertia, (void**)&d_bond, (void**)&b.nbr, (void**)&b.ncnt, (void**)&b.posw};
+                       (void**)&d_inertia, (void**)&d_bond, (void**)&b.nbr, (void**)&b.ncnt, (void**)&b.posw,
+                       (void**)&b.img};
     for (void** a : arrays) {
       dfree(*a);
       *a = nullptr;
     }
     b.nl_cap = 0;
     nl_alloc_p = 0;
+    nl_alloc_ints = 0;
     size_t p4 = sizeof(float4) * (size_t)cap, p1 = sizeof(int32_t) * (size_t)cap;
     size_t pd = sizeof(float) * (size_t)cap * dim;
     size_t pa = sizeof(float) * (size_t)cap * (dim == 3 ? 3 : 1);
@@ -345,6 +347,11 @@ int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* h
     }
     if (d.domain == DOM_FREE) any_free = true;
     choose_grid(sp, dim, rmax_s[s], skin, d.n, lo, hi);
+    // list cutoff widening: a few float32 ulps of the largest coordinate the
+    // list build subtracts (wrapped positions plus a box-length image shift)
+    float ext = 0.0f;
+    for (int a = 0; a < dim; ++a) ext = std::max(ext, std::fabs(sp.anchor[a]) + 2.0f * sp.box[a]);
+    sp.nl_eps = 8.0f * ext * 5.9604645e-8f;
     sp.c0 = c_total;
     c_total += sp.ncap;
     if (c_total >= (1LL << 31) - 2)
@@ -371,8 +378,12 @@ int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* h
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.sys, sys_h.data(), sizeof(SysParams) * S, cudaMemcpyHostToDevice, stream));
   JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
   if (!use_nl) return plan_list(0);
+  int rc_t = plan_tiles();
+  if (rc_t) return rc_t;
   // Verlet-list capacity: expected neighbours within 2 r_max + skin at the
-  // densest system, plus eight standard deviations of a Poisson count.
+  // densest system, plus six standard deviations of a Poisson count.  A row
+  // that overflows switches the steps to the cell traversal (still exact)
+  // until the host doubles the capacity.
   double mean_max = 0.0;
   for (int s = 0; s < S; ++s) {
     const SysParams& sp = sys_h[s];
@@ -384,35 +395,141 @@ int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* h
     double mean = desc[s].n / vol * sphere;
     mean_max = std::max(mean_max, mean);
   }
-  int cap = (int)std::ceil(mean_max + 8.0 * std::sqrt(mean_max) + 16.0);
+  int cap = (int)std::ceil(mean_max + 6.0 * std::sqrt(mean_max) + 8.0);
   cap = std::min(256, (cap + 7) / 8 * 8);
   if (nl_request > 0) cap = nl_request;
   return plan_list(cap);
 }
 
-// (Re)allocate the Verlet list for cap entries per slot (0: no list).
+// Tiles of the brick list build (jdem_tiles.cu) for every system: bricks of
+// cells holding about 240 particles, near-cubic so the staged stencil region
+// (the brick grown by one cell per side) is small against the brick; a system
+// smaller than one brick is one tile.  Free domains re-grid on the device at
+// every re-sort, so a handle with one keeps the per-slot list build (no tiles).
+int JdemHandle::plan_tiles() {
+  std::vector<TileDesc> t;
+  int nst = 0, nv = 0, nrows = 0;
+  if (!any_free && use_nl) {
+    const double TT = 240.0;
+    constexpr long long kMaxNV = 2048, kMaxHomeRows = 256, kMaxRows = 512;
+    double stage_max = 0.0;
+    long long nv_max = 0, rows_max = 0;
+    for (int s = 0; s < S; ++s) {
+      if (desc[s].n == 0) continue;
+      const SysParams& sp = sys_h[s];
+      const long long g[3] = {sp.g[0], sp.g[1], dim == 3 ? sp.g[2] : 1};
+      const double cells = (double)g[0] * (double)g[1] * (double)g[2];
+      const double occ = (double)desc[s].n / cells;
+      const bool per = sp.domain == DOM_PERIODIC;
+      int flags = (per && (g[0] < 3 || g[1] < 3 || (dim == 3 && g[2] < 3))) ? TILE_DIRECT : 0;
+      // Unflagged list entries skip the minimum image: a pair in the same image
+      // stays within r_i + r_j + 2 skin <= cell + skin while the list lives,
+      // which must be below half the smallest box edge.
+      float bmin = sp.box[0];
+      for (int a = 1; a < dim; ++a) bmin = std::min(bmin, sp.box[a]);
+      if (per && !(1.01f * (sp.cell_bin + skin) < 0.5f * bmin)) flags |= TILE_ALLIMAGE;
+      // brick edge lengths in cells
+      const double V = std::max(1.0, TT / std::max(occ, 1e-12));
+      long long e[3];
+      if (dim == 3) {
+        const double side = std::cbrt(V);
+        e[2] = std::min(g[2], std::max(1LL, (long long)std::llround(side)));
+        e[1] = std::min(g[1], std::max(1LL, (long long)std::llround(side)));
+        e[0] = std::min(g[0], std::max(1LL, (long long)std::llround(V / (double)(e[1] * e[2]))));
+      } else {
+        const double side = std::sqrt(V);
+        e[2] = 1;
+        e[1] = std::min(g[1], std::max(1LL, (long long)std::llround(side)));
+        e[0] = std::min(g[0], std::max(1LL, (long long)std::llround(V / (double)e[1])));
+      }
+      while (e[1] * e[2] > kMaxHomeRows) {
+        if (e[1] >= e[2]) e[1] = (e[1] + 1) / 2;
+        else e[2] = (e[2] + 1) / 2;
+      }
+      long long nb[3];
+      for (int a = 0; a < 3; ++a) nb[a] = (g[a] + e[a] - 1) / e[a];
+      for (long long kz = 0; kz < nb[2]; ++kz)
+        for (long long ky = 0; ky < nb[1]; ++ky)
+          for (long long kx = 0; kx < nb[0]; ++kx) {
+            TileDesc d{};
+            d.sys = s;
+            d.x0 = (int)(kx * g[0] / nb[0]);
+            d.x1 = (int)((kx + 1) * g[0] / nb[0]);
+            d.y0 = (int)(ky * g[1] / nb[1]);
+            d.y1 = (int)((ky + 1) * g[1] / nb[1]);
+            d.z0 = (int)(kz * g[2] / nb[2]);
+            d.z1 = (int)((kz + 1) * g[2] / nb[2]);
+            d.flags = flags;
+            t.push_back(d);
+            const long long v = (long long)(d.x1 - d.x0 + 2) * (d.y1 - d.y0 + 2) * (dim == 3 ? d.z1 - d.z0 + 2 : 1);
+            const long long rows = (long long)(d.y1 - d.y0 + 2) * (dim == 3 ? d.z1 - d.z0 + 2 : 1);
+            if (!flags && v <= kMaxNV && rows <= kMaxRows) {
+              nv_max = std::max(nv_max, v);
+              rows_max = std::max(rows_max, rows);
+              stage_max = std::max(stage_max, (double)v * occ);
+            }
+          }
+      if ((long long)t.size() > (1LL << 30)) return fail(JDEM_ERR_CAPACITY_OVERFLOW, "too many list tiles");
+    }
+    nv = (int)std::max(nv_max, 32LL);
+    nrows = (int)std::max(rows_max, 9LL);
+    nst = (int)std::min(4096.0, std::max(512.0, std::ceil((1.35 * stage_max + 64.0) / 256.0) * 256.0));
+  }
+  const bool same = t.size() == tiles_h.size() && nst == b.tb_nst && nv == b.tb_nv && nrows == b.tb_nrows &&
+                    (t.empty() || std::memcmp(t.data(), tiles_h.data(), sizeof(TileDesc) * t.size()) == 0);
+  if (!same) {
+    drop_graphs();
+    if ((long long)t.size() > tiles_alloc) {
+      dfree(d_tiles);
+      d_tiles = nullptr;
+      tiles_alloc = 0;
+      int rc = dalloc((void**)&d_tiles, sizeof(TileDesc) * t.size());
+      if (rc) return rc;
+      tiles_alloc = (long long)t.size();
+    }
+    if (!t.empty())
+      JDEM_CUDA_TRY(this, cudaMemcpy(d_tiles, t.data(), sizeof(TileDesc) * t.size(), cudaMemcpyHostToDevice));
+    tiles_h.swap(t);
+  }
+  b.tiles = d_tiles;
+  b.n_tiles = (int)tiles_h.size();
+  b.tb_nst = nst;
+  b.tb_nv = nv;
+  b.tb_nrows = nrows;
+  return JDEM_OK;
+}
+
+// (Re)allocate the Verlet list for cap entries per slot (0: no list), one
+// cap x 32 block of entries per warp of slots.
 int JdemHandle::plan_list(int cap) {
-  if (cap == b.nl_cap && (cap == 0 || (b.nbr && P <= nl_alloc_p))) return JDEM_OK;
+  cap = std::min(cap, kMaxListCap);
+  const long long need = cap <= 0 ? 0 : ((P + 31) / 32) * 32LL * cap;
+  if (cap > 0 && b.n_tiles > 0 && prepare_tbuild(tbuild_smem(b.tb_nst, b.tb_nv, b.tb_nrows)))
+    return fail(JDEM_ERR_CUDA, "cannot raise shared memory for the list build");
+  if (cap == b.nl_cap && (cap == 0 || (b.nbr && need <= nl_alloc_ints && P <= nl_alloc_p))) return JDEM_OK;
   drop_graphs();
   dfree(b.nbr);
   dfree(b.ncnt);
   b.nbr = nullptr;
   b.ncnt = nullptr;
   b.nl_cap = 0;
+  nl_alloc_ints = 0;
   b.nl_skin = skin;
   if (cap <= 0 || P == 0) return JDEM_OK;
-  cap = std::min(cap, kMaxListCap);
-  if (prepare_nlbuild(cap)) return fail(JDEM_ERR_CUDA, "cannot raise shared memory for the list build");
   int rc;
-  // sliced layout: one cap x 32 block per warp of slots
-  size_t slices = (size_t)((P + 31) / 32);
-  if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)cap * 32 * slices))) return rc;
+  if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)need))) return rc;
   if ((rc = dalloc((void**)&b.ncnt, sizeof(int32_t) * (size_t)P))) return rc;
+  // empty rows until the first build
+  JDEM_CUDA_TRY(this, cudaMemsetAsync(b.ncnt, 0, sizeof(int32_t) * (size_t)P, stream));
   dfree(b.posw);
+  dfree(b.img);
   b.posw = nullptr;
+  b.img = nullptr;
   if ((rc = dalloc((void**)&b.posw, sizeof(float4) * (size_t)P))) return rc;
+  if ((rc = dalloc((void**)&b.img, sizeof(int32_t) * (size_t)P))) return rc;
   b.nl_cap = cap;
   nl_alloc_p = P;
+  nl_alloc_ints = need;
   return JDEM_OK;
 }
 
@@ -738,8 +855,10 @@ int JdemHandle::sync_status() {
     int grown = std::min(kMaxListCap, std::max(16, 2 * b.nl_cap));
     int rc = grown > b.nl_cap ? plan_list(grown) : JDEM_OK;
     if (rc) return rc;
+    // a full re-sort: it refreshes the wrapped positions the new list build reads
     unsigned int st = c->status & ~(unsigned int)ST_NL_OVERFLOW, one = 1u;
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->status, &st, 4, cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->need_rebuild, &one, 4, cudaMemcpyHostToDevice, stream));
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->nl_dirty, &one, 4, cudaMemcpyHostToDevice, stream));
     JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
     nl_regrowths += 1;
@@ -765,6 +884,7 @@ int JdemHandle::sync_status() {
     bbox_pending = false;
   }
   if (c->status & ST_NONFINITE) return fail(JDEM_ERR_NONFINITE, "non-finite position or velocity");
+
   return JDEM_OK;
 }
 
@@ -1025,6 +1145,9 @@ int jdem_stats(JdemHandle* h, JdemStats* out) {
   out->device_status = h->sticky_status;
   out->graphs = (int32_t)h->graphs.size();
   out->device_bytes = h->device_bytes;
+  out->list_regrowths = h->nl_regrowths;
+  out->list_capacity = h->b.nl_cap;
+  out->list_tiles = h->b.n_tiles;
   return JDEM_OK;
 }
 

@@ -18,6 +18,10 @@ struct JdemHandle {
   long long c_cap = 0;  // allocated cell capacity
   int s_cap = 0;        // allocated system capacity
   long long nl_alloc_p = 0;
+  long long nl_alloc_ints = 0;  // allocated Verlet-list entries
+  std::vector<jdem::TileDesc> tiles_h;
+  jdem::TileDesc* d_tiles = nullptr;
+  long long tiles_alloc = 0;
   float skin = 0.0f;
   int chunk = 50;
   int n_mat = 1;
@@ -76,6 +80,7 @@ struct JdemHandle {
   int plan_grid(const float* rmax_s, const float* lo_s, const float* hi_s);
   int upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
                       const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s);
+  int plan_tiles();
   int plan_list(int cap);
   int reset_ctl();
   int upload(const JdemHostState* s, bool device_ptrs);

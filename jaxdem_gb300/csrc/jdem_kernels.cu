@@ -13,29 +13,11 @@
 // a compensated (two-sum) accumulator, so results are deterministic.
 #include "jdem_device.cuh"
 #include "jdem_kernels.h"
+#include "jdem_pair.cuh"
 
 namespace jdem {
 
 // ---------------------------------------------------------------- utilities
-
-template <typename T>
-__device__ __forceinline__ T warp_max(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    T w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = v > w ? v : w;
-  }
-  return v;
-}
-
-// Warp max of the squared displacement; lane 0 raises the kernel-wide
-// maximum only when it exceeds the value already recorded, so the atomic is
-// rare.  No thread waits on another; k_fin folds the maximum in afterwards.
-__device__ __forceinline__ void warp_disp(Ctl* ctl, float d2) {
-  d2 = warp_max(d2);
-  if ((threadIdx.x & 31) == 0 && d2 > 0.0f && d2 > __uint_as_float(__ldcg(&ctl->maxdisp2)))
-    atomicMax(&ctl->maxdisp2, __float_as_uint(d2));
-}
 
 // After a kernel that moved particles: bound += max displacement, raise
 // need_rebuild past skin / 2; after a force kernel also flip the position
@@ -323,15 +305,26 @@ __global__ void k_gather(Bufs b) {
     const float4 p = b.pos[ps][t];
     b.pos[ps ^ 1u][u] = p;
     if (b.posw) {
-      // positions wrapped into the primary box, for the list build only
+      // positions wrapped into the primary box and the image they came from,
+      // for the list build only
       const SysParams& sp = b.sys[b.tag[sel][t] & TAG_SYS_MASK];
       float4 w = p;
+      int32_t im = 0;
       if (sp.domain == DOM_PERIODIC) {
-        w.x = p.x - sp.box[0] * floorf((p.x - sp.anchor[0]) / sp.box[0]);
-        w.y = p.y - sp.box[1] * floorf((p.y - sp.anchor[1]) / sp.box[1]);
-        w.z = p.z - sp.box[2] * floorf((p.z - sp.anchor[2]) / sp.box[2]);
+        const float kx = floorf((p.x - sp.anchor[0]) / sp.box[0]);
+        const float ky = floorf((p.y - sp.anchor[1]) / sp.box[1]);
+        const float kz = floorf((p.z - sp.anchor[2]) / sp.box[2]);
+        w.x = p.x - sp.box[0] * kx;
+        w.y = p.y - sp.box[1] * ky;
+        w.z = p.z - sp.box[2] * kz;
+        if (fabsf(kx) < 500.0f && fabsf(ky) < 500.0f && fabsf(kz) < 500.0f) {
+          im = ((int)kx + 512) | (((int)ky + 512) << 10) | (((int)kz + 512) << 20);
+        } else {
+          im = (1 << 30) | (int)(u & 0x3FFFFFFF);  // far image: unique, never equal to another's
+        }
       }
       b.posw[u] = w;
+      if (b.img) b.img[u] = im;
     }
     b.vel[sel ^ 1u][u] = b.vel[sel][t];
     // forces are not moved: every re-sort is followed by a force kernel that
@@ -412,55 +405,6 @@ __global__ void k_pre(Bufs b, int mode) {
 
 // ---------------------------------------------------------- fused step
 
-// Visit every slot binned in the unique stencil cells of a slot's cell
-// (cell_list.py:66-96 stencil, deduplicated for small periodic grids).  The
-// three cells of a stencil row along x form at most two contiguous slot ranges.
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_candidate(const int32_t* __restrict__ cs, const SysParams& sp,
-                                                   long long local, F&& f) {
-  const bool per = sp.domain == DOM_PERIODIC;
-  const int gx = sp.g[0], gy = sp.g[1];
-  int cx = (int)(local % gx);
-  long long rem = local / gx;
-  int cy = (int)(rem % gy);
-  int cz = DIM == 3 ? (int)(rem / gy) : 0;
-  int ys[3], zs[3];
-  int ny = axis_set(cy, gy, per, ys);
-  int nz = DIM == 3 ? axis_set(cz, sp.g[2], per, zs) : 1;
-  if (DIM == 2) zs[0] = 0;
-  int xa0, xb0, xa1, xb1;
-  x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
-  for (int iz = 0; iz < nz; ++iz) {
-    for (int iy = 0; iy < ny; ++iy) {
-      long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
-      int ja = cs[row + xa0], jb = cs[row + xb0];
-      for (int j = ja; j < jb; ++j) f(j);
-      if (xa1 < xb1) {
-        ja = cs[row + xa1];
-        jb = cs[row + xb1];
-        for (int j = ja; j < jb; ++j) f(j);
-      }
-    }
-  }
-}
-
-// Minimum-image displacement and squared distance, in the reference's order.
-template <int DIM>
-__device__ __forceinline__ float pair_disp(const SysParams& sp, bool per, float4 pi, float4 pj, float& dx,
-                                           float& dy, float& dz) {
-  dx = pi.x - pj.x;
-  dy = pi.y - pj.y;
-  dz = DIM == 3 ? pi.z - pj.z : 0.0f;
-  if (per) {
-    dx = dx - sp.box[0] * rintf(dx * sp.inv_box[0]);
-    dy = dy - sp.box[1] * rintf(dy * sp.inv_box[1]);
-    if (DIM == 3) dz = dz - sp.box[2] * rintf(dz * sp.inv_box[2]);
-  }
-  float dsq = dx * dx + dy * dy;
-  if (DIM == 3) dsq = dsq + dz * dz;
-  return dsq;
-}
-
 // Verlet list of every slot, built right after a re-sort: all j with
 // |r_ij| < r_i + r_j + skin.  While the displacement bound stays below
 // skin / 2 every contact of the following steps is in the list.  One thread
@@ -486,6 +430,8 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
   const float skin = b.nl_skin;
   const int cap = b.nl_cap;
   int32_t* __restrict__ out = b.nbr + ((t >> 5) * cap) * 32 + (t & 31);
+  // every periodic entry keeps the minimum image in the force kernel
+  const uint32_t mark = per ? kEntryImage : 0u;
   int n = 0;
   auto range = [&](int ja, int jb, float sx, float sy, float sz) {
     for (int j = ja; j < jb; j += 4) {
@@ -510,7 +456,7 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
           }
           float rc = (pi.w + q[u].w + skin) * 1.0001f;
           if (dsq < rc * rc) {
-            if (n < cap) out[n * 32] = jj;
+            if (n < cap) out[n * 32] = (int32_t)((uint32_t)jj | mark);
             ++n;
           }
         }
@@ -556,133 +502,21 @@ __global__ void k_cond(const Ctl* ctl, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, v ? 1u : 0u);
 }
 
-// One thread per slot.  Contact force (spring.py:97-108 with the periodic
-// minimum image of periodic.py:74-79), from the Verlet list when NL is set
-// and the list is complete, else from the stencil cells; then ForceManager
-// gravity (force_manager.py:393-405), step_after_force, and, in MODE_STEP,
-// the next step's ReflectDomain.apply, step_before_force and drift.
+// One thread per slot (slot-order path: free domains, or no list): the fused
+// per-particle step of jdem_pair.cuh, from the slot-indexed Verlet list when NL
+// is set and the list is complete, else from the stencil cells.
 template <int DIM, bool NL, bool GENERAL>
 __global__ void __launch_bounds__(256, 4) k_force(Bufs b, int mode) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   const bool use_list = NL && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
-  int base_mode = mode & 7;
   float d2max = 0.0f;
   if (t < b.P) {
-    const float4* __restrict__ P = b.pos[ps];
-    const float4 pi = P[t];
-    const uint32_t tg = b.tag[sel][t];
-    const int s = tg & TAG_SYS_MASK;
-    const SysParams& sp = b.sys[s];
-    const bool per = sp.domain == DOM_PERIODIC;
-    const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
-    const float k0 = b.young[mat_i * b.n_mat + mat_i];
-    // GENERAL: several materials or bond exclusions (valid_interaction_mask,
-    // colliders/__init__.py:225-243); otherwise both checks compile away
-    const bool multi_mat = GENERAL && b.n_mat > 1;
-    const bool bonds = GENERAL && b.bond_w > 0 && !b.interact_same_bond;
-    const int oi = bonds ? b.orig[sel][t] : 0;
-    float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
-    auto pair = [&](int j, const float4& pj) {
-      float dx, dy, dz;
-      float dsq = pair_disp<DIM>(sp, per, pi, pj, dx, dy, dz);
-      float R = pi.w + pj.w;
-      if (dsq < R * R * 1.000001f && j != (int)t) {
-        float k = k0;
-        if (multi_mat) {
-          int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
-          k = b.young[mat_i * b.n_mat + mat_j];
-        }
-        if (bonds) {
-          int oj = b.orig[sel][j];
-          bool bonded = false;
-          for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
-          if (bonded) return;
-        }
-        float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
-        float rr = dsq * inv;
-        float delta = R - rr;
-        delta = delta > 0.0f ? delta : 0.0f;
-        float mag = k * delta * inv;
-        two_sum_acc(fx, ex, mag * dx);
-        two_sum_acc(fy, ey, mag * dy);
-        if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
-      }
-    };
-    if (use_list) {
-      const int n = b.ncnt[t];
-      const int32_t* __restrict__ nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
-      for (int k = 0; k < n; k += 4) {
-        int jj[4];
-        float4 q[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) jj[u] = k + u < n ? nb[(k + u) * 32] : (int)t;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) q[u] = P[jj[u]];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) pair(jj[u], q[u]);
-      }
-    } else {
-      for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) { pair(j, P[j]); });
-    }
-    float F[3] = {fx + ex, fy + ey, DIM == 3 ? fz + ez : 0.0f};
-    if (base_mode == MODE_FORCE_ONLY) {
-      b.frc[sel][t] = make_float4(F[0], F[1], F[2], 0.0f);
-    } else {
-      float4 v4 = b.vel[sel][t];
-      float m = v4.w;
-      bool fixed = (tg & TAG_FIXED) != 0u;
-      float fr = fixed ? 0.0f : 1.0f;
-      float p[3] = {pi.x, pi.y, pi.z}, v[3] = {v4.x, v4.y, v4.z};
-      // ForceManager.apply: F_contact + F_part(0) + gravity * (mass / count)
-#pragma unroll
-      for (int a = 0; a < DIM; ++a) F[a] = (F[a] + 0.0f) + sp.gravity[a] * (m / 1.0f);
-      if (sp.lin == LIN_VERLET) {
-        float sc = sp.dt * 0.5f / m;
-#pragma unroll
-        for (int a = 0; a < DIM; ++a) v[a] = v[a] + F[a] * sc * fr;
-      } else if (sp.lin == LIN_EULER) {
-        float sc = sp.dt / m;
-#pragma unroll
-        for (int a = 0; a < DIM; ++a) {
-          v[a] = v[a] + F[a] * sc * fr;
-          p[a] = p[a] + sp.dt * v[a];
-        }
-      }
-      b.frc[sel][t] = make_float4(F[0], F[1], F[2], 0.0f);
-      if (base_mode == MODE_STEP) {
-        if ((mode & MODE_BBOX) && sp.domain == DOM_FREE) {
-#pragma unroll
-          for (int a = 0; a < DIM; ++a) {
-            atomicMin((unsigned int*)&b.bbox[s * 6 + a], f2ord(p[a] - pi.w));
-            atomicMax((unsigned int*)&b.bbox[s * 6 + 3 + a], f2ord(p[a] + pi.w));
-          }
-        }
-        if (sp.domain == DOM_REFLECT) reflect_sphere<DIM>(sp, p, v, F, pi.w, m, fixed);
-        if (sp.lin == LIN_VERLET) {
-          float sc = sp.dt * 0.5f / m;
-#pragma unroll
-          for (int a = 0; a < DIM; ++a) {
-            v[a] = v[a] + F[a] * sc * fr;
-            p[a] = p[a] + sp.dt * v[a];
-          }
-        }
-      }
-      float pa[3] = {pi.x, pi.y, pi.z};
-#pragma unroll
-      for (int a = 0; a < DIM; ++a) {
-        float d = p[a] - pa[a];
-        d2max = d2max + d * d;
-      }
-      b.pos[ps ^ 1u][t] = make_float4(p[0], p[1], p[2], pi.w);
-      b.vel[sel][t] = make_float4(v[0], v[1], v[2], m);
-      if (!(d2max == d2max) || d2max > 3.0e38f) {
-        atomicOr(&b.ctl->status, ST_NONFINITE);
-        d2max = 0.0f;
-      }
-    }
+    const int n = use_list ? b.ncnt[t] : 0;
+    const int32_t* nb = use_list ? b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31) : nullptr;
+    d2max = particle_step<DIM, GENERAL>(b, mode, t, sel, ps, use_list, nb, n, 32);
   }
-  if (base_mode != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
+  if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
 }
 
 // -------------------------------------------------------------- rotation
@@ -1063,12 +897,12 @@ void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
   launch_fin(b, false, false, 0, st);
 }
 
-size_t nlbuild_smem(int cap) { return 0; }
-
-int prepare_nlbuild(int cap) { return 0; }
-
 void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st) {
   if (b.P == 0 || b.nl_cap <= 0) return;
+  if (b.n_tiles > 0) {
+    launch_tbuild(dim, b, st);
+    return;
+  }
   if (dim == 3) k_nlbuild<3><<<nblk(b.P, 256), 256, 0, st>>>(b);
   else k_nlbuild<2><<<nblk(b.P, 256), 256, 0, st>>>(b);
 }

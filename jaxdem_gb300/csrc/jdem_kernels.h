@@ -17,8 +17,10 @@ int rebuild_kernel_count(bool any_free);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st);
-size_t nlbuild_smem(int cap);
-int prepare_nlbuild(int cap);
+// brick list build (jdem_tiles.cu)
+size_t tbuild_smem(int nst, int nv, int nrows);
+int prepare_tbuild(size_t bytes);
+void launch_tbuild(int dim, const Bufs& b, cudaStream_t st);
 void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st);
 // After k_pre / k_force: fold the displacement into the bound (see k_fin).
 void launch_fin(const Bufs& b, bool after_force, bool set_cond, cudaGraphConditionalHandle h, cudaStream_t st);
