@@ -203,6 +203,7 @@ def peaks():
 def run_ours(args, rank, world, dist):
     import torch
 
+    from jaxdem_gb300 import replicas
     from jaxdem_gb300 import workloads as W
     from jaxdem_gb300._lib import Engine, host_register, host_unregister
 
@@ -260,10 +261,7 @@ def run_ours(args, rank, world, dist):
     if dist is not None:
         dist.barrier()
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(dist, total_ms, device=f"cuda:{dev}")
     stats = eng.stats()
 
     # instrumented pass: per-launch events around the fused force kernel
@@ -303,7 +301,7 @@ def run_ours(args, rank, world, dist):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_seconds)
 
-    value = world * w.N * K / (total_ms * 1e-3)
+    value = replicas.aggregate_throughput([w.N * K] * world, total_ms * 1e-3)
     # per call: k_pre; per step: k_cond + k_force; per re-sort: 7 sort kernels + the list build
     rebuilds_timed = stats["rebuilds"] - rebuilds_before
     launches = sum(1 + 2 * c for c in chunks) + 8 * rebuilds_timed
