@@ -20,7 +20,7 @@ from typing import Callable, Optional, Sequence
 
 import numpy as np
 
-CANDIDATES = (0.15, 0.3, 0.45, 0.65, 0.9)  # in units of r_max
+CANDIDATES = (0.15, 0.3, 0.45, 0.65, 0.9, 1.2)  # in units of r_max
 CACHE = Path(os.environ.get("JDEM_TUNE_CACHE", Path.home() / ".cache" / "jaxdem_gb300" / "tune.json"))
 
 
