@@ -142,3 +142,84 @@ class NaiveSimulator(Collider):
         e = session.energies(state, system)
         pe = e[..., 0]
         return state, system, (F32(pe) if np.ndim(pe) == 0 else pe.astype(F32))
+
+
+@Collider.register("NeighborList")
+@dataclass
+class NeighborList(Collider):
+    """Verlet neighbour-list collider (``colliders/neighbor_list.py:134-``).
+
+    Candidates within ``cutoff + skin`` are cached and rebuilt once the
+    largest displacement since the last build exceeds ``skin / 2``
+    (``neighbor_list.py:58-131``).  The device engine runs exactly this scheme
+    for every collider, with a per-pair list cutoff ``r_i + r_j + skin``, so
+    this type selects the same device path with the caller's skin and initial
+    list capacity.  The list lives on the device; ``create_neighbor_list``
+    returns the reference's padded ``(N, max_neighbors)`` form.
+
+    Spheres interact within ``r_i + r_j``, so the reference misses contacts
+    when ``cutoff`` is below ``2 max(rad)``; the device list never misses a
+    contact and such a cutoff is rejected rather than silently changing the
+    force.
+    """
+
+    cutoff: Any = None
+    skin: Any = None
+    max_neighbors: Any = None
+    secondary_collider_type: str = "CellList"
+
+    @classmethod
+    def Create(cls, state, cutoff: float, skin: Optional[float] = None, skin_fraction: Optional[float] = None,
+               max_neighbors: Optional[int] = None, number_density: float = 1.0, safety_factor: float = 1.2,
+               secondary_collider_type: str = "CellList", secondary_collider_kw: Optional[dict] = None):
+        """``NeighborList.Create`` (``neighbor_list.py:287-440``): absolute ``skin`` or
+        ``skin_fraction`` of the cutoff (default 0.05), and the neighbour-count estimate
+        ``ceil(safety_factor * V(cutoff + skin) * density)`` when ``max_neighbors`` is
+        not given."""
+        if skin is not None and skin_fraction is not None:
+            raise ValueError("Pass either `skin` (absolute distance) or `skin_fraction` "
+                             "(fraction of the cutoff), not both.")
+        cutoff = float(cutoff)
+        skin_val = float(skin) if skin is not None else float(0.05 if skin_fraction is None else skin_fraction) * cutoff
+        rad = np.asarray(state._rad, F32)
+        rmax = float(rad.max()) if rad.size else 0.0
+        if F32(cutoff) < F32(2.0) * F32(rmax):  # float32, as the state's radii
+            raise NotImplementedError(
+                f"NeighborList cutoff {cutoff:g} is below the largest contact distance {2 * rmax:g}: the "
+                "reference would miss those contacts, the GB300 list does not")
+        if max_neighbors is None:
+            list_cutoff = cutoff + skin_val
+            pos = np.asarray(state.pos, np.float64).reshape(-1, state.dim)
+            if pos.size:
+                ext = np.maximum(pos.max(axis=0) - pos.min(axis=0) + 2.0 * rmax, 1.0)
+                density = max(float(number_density), pos.shape[0] / float(np.prod(ext)))
+            else:
+                density = float(number_density)
+            vol = np.pi * list_cutoff ** state.dim * (1.0 if state.dim == 2 else 4.0 / 3.0)
+            max_neighbors = max(1, int(np.ceil(safety_factor * vol * density)))
+        return cls(cutoff=F32(cutoff), skin=F32(skin_val), max_neighbors=int(max_neighbors),
+                   secondary_collider_type=str(secondary_collider_type))
+
+    @staticmethod
+    def compute_force(state, system):
+        """``neighbor_list.py:594-672`` on the GPU (rebuild when due, then the list sum)."""
+        from . import session
+
+        return session.compute_force(state, system)
+
+    @staticmethod
+    def compute_potential_energy(state, system):
+        """``neighbor_list.py:674-734`` on the GPU; returns ``(state, system, energy)``."""
+        from . import session
+
+        e = session.energies(state, system)
+        pe = e[..., 0]
+        return state, system, (F32(pe) if np.ndim(pe) == 0 else pe.astype(F32))
+
+    @staticmethod
+    def create_neighbor_list(state, system, cutoff: float, max_neighbors: int):
+        """``neighbor_list.py:485-543`` on the GPU: ``(state, system, nl, overflow)``."""
+        from . import session
+
+        nl, ovf = session.neighbor_list(state, system, cutoff, max_neighbors)
+        return state, system, nl, ovf

@@ -220,7 +220,6 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
   const float4* __restrict__ P = b.pos[ps];
   const float4 pi = P[t];
   const uint32_t tg = b.tag[sel][t];
-  const float4 v4 = b.vel[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
   ContactSum<DIM, GENERAL> acc(b, sp, pi, tg, sel, t);
   if (use_list) {
@@ -242,6 +241,8 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
     });
   }
   float F[3] = {acc.fx + acc.ex, acc.fy + acc.ey, DIM == 3 ? acc.fz + acc.ez : 0.0f};
+  // loaded after the contact loop: holding it through the loop costs registers
+  const float4 v4 = (mode & 7) == MODE_FORCE_ONLY ? make_float4(0.f, 0.f, 0.f, 0.f) : b.vel[sel][t];
   return integrate_particle<DIM>(b, mode, t, sel, ps, sp, pi, tg, v4, F);
 }
 

@@ -42,7 +42,7 @@ def _check_supported(state: State, system) -> None:
     if system.force_model.type_name != "spring":
         raise NotImplementedError(f"force model '{system.force_model.type_name}' is not on the GB300 hot path")
     coll = system.collider.type_name
-    if coll not in ("celllist", "naive", "celllistgb300"):
+    if coll not in ("celllist", "naive", "celllistgb300", "neighborlist"):
         raise NotImplementedError(f"collider '{coll}' is not supported by the GB300 engine")
     _domain_key(system)
     if system.linear_integrator.type_name not in LINEAR:
@@ -117,14 +117,17 @@ def engine_for(state: State, system) -> Engine:
     young = np.asarray(system.mat_table.young_eff, F32)
     W = _bond_width(state)
     skin = _skin(state, system)
-    key = (state.dim, W, bool(system.interact_same_bond_id), round(skin, 7), young.tobytes(),
+    # a NeighborList collider's max_neighbors is the initial list capacity
+    cap = getattr(system.collider, "max_neighbors", None)
+    nl = int(cap) if cap else True
+    key = (state.dim, W, bool(system.interact_same_bond_id), round(skin, 7), nl, young.tobytes(),
            tuple((d["n"], d["domain"], d["linear"], d["rotation"], d["dt"], tuple(map(float, d["box_size"])),
                   tuple(map(float, d["anchor"])), d["restitution"], tuple(map(float, d["gravity"])),
                   d["cell_size"], d["search_range"]) for d in descs))
     eng = _CACHE.get(key)
     if eng is None:
         eng = Engine(state.dim, descs, young, skin=skin, bond_width=W,
-                     interact_same_bond_id=bool(system.interact_same_bond_id))
+                     interact_same_bond_id=bool(system.interact_same_bond_id), neighbor_list=nl)
         _CACHE[key] = eng
         while len(_CACHE) > _CACHE_MAX:
             _, old = _CACHE.popitem(last=False)

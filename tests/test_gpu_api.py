@@ -108,3 +108,22 @@ def test_collider_slot_and_pair_forces():
     want = {tuple(p) for p in R.contact_pairs(ost, osy).tolist()}
     assert got == want
     assert np.array_equal(jdem.utils.contact_pairs(st, sy), R.contact_pairs(ost, osy))
+
+
+def test_neighbor_list_collider_steps_like_cell_list():
+    """The NeighborList collider type (colliders/neighbor_list.py) runs the same device
+    path with its own skin and initial capacity: same trajectory as CellList."""
+    w, st, sy = make(N=1500, seed=11, phi=0.5)
+    mats = [jdem.Material.create("elastic", young=1e3, poisson=0.3, density=1.0)]
+    table = jdem.MaterialTable.from_materials(mats)
+    sy_nl = jdem.System.create(state=st, collider_type="NeighborList", collider_kw=dict(cutoff=1.2, skin=0.2),
+                               domain_type="periodic", mat_table=table, dt=1e-3,
+                               domain_kw=dict(box_size=w.box_size, anchor=w.anchor))
+    a, _ = jdem.System.step(st, sy, n=40)
+    b, sy_b = jdem.System.step(st, sy_nl, n=40)
+    assert min_image_diff(b.pos_c, a.pos_c, w.box_size) <= 1e-5
+    assert force_err(b.force, a.force) <= 1e-4
+    assert int(sy_b.step_count) == 40
+    _, _, pe = sy_nl.collider.compute_potential_energy(b, sy_b)
+    _, _, pe_ref = sy.collider.compute_potential_energy(b, sy)
+    assert np.isclose(pe, pe_ref, rtol=1e-5)

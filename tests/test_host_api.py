@@ -122,3 +122,24 @@ def test_grid_state_lattice():
     assert st.pos_c.shape == (6, 2)
     assert np.allclose(sorted(set(st.pos_c[:, 1].tolist())), [0.0, 1.5, 3.0])
     assert np.all((st.vel >= -1) & (st.vel <= 1))
+
+
+def test_neighbor_list_collider_create():
+    """NeighborList.Create (colliders/neighbor_list.py:287-440): absolute skin or a
+    fraction of the cutoff (default 0.05), not both; the estimated max_neighbors; a
+    cutoff below the largest contact distance is refused (the device list never drops
+    contacts, the reference would)."""
+    import jaxdem_gb300 as jdem
+
+    rng = np.random.default_rng(0)
+    st = jdem.State.create(pos=rng.uniform(0, 10, (200, 3)), rad=np.full(200, 0.5))
+    c = jdem.Collider.create("NeighborList", state=st, cutoff=1.0, skin=0.2)
+    assert type(c).__name__ == "NeighborList" and c.type_name == "neighborlist"
+    assert np.isclose(c.skin, 0.2) and np.isclose(c.cutoff, 1.0) and c.max_neighbors >= 1
+    assert np.isclose(jdem.Collider.create("NeighborList", state=st, cutoff=1.2).skin, 0.06)
+    assert np.isclose(jdem.Collider.create("NeighborList", state=st, cutoff=1.0, skin_fraction=0.5).skin, 0.5)
+    with pytest.raises(ValueError):
+        jdem.Collider.create("NeighborList", state=st, cutoff=1.0, skin=0.1, skin_fraction=0.1)
+    with pytest.raises(NotImplementedError):
+        jdem.Collider.create("NeighborList", state=st, cutoff=0.8)
+    assert jdem.Collider.create("NeighborList", state=st, cutoff=1.0, max_neighbors=17).max_neighbors == 17
