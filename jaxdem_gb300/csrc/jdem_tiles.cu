@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
           w.x = w.x + sx[k];
           w.y = w.y + syz[0];
           if (DIM == 3) w.z = w.z + syz[1];
+          w.w = w.w * 1.0001f;  // radius with the list cutoff's relative widening
           spos[o + i] = w;
           sslot[o + i] = ja + i;
           simg[o + i] = b.img[ja + i] | shifted;
@@ -291,7 +292,8 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
     const int ix = last_le(vstart, rb + 1, rb + bk.W + 1, oh) - rb;  // virtual x of the home cell
     const long long slot = sslot[oh];
     const float4 pi = spos[oh];
-    const float base_r = pi.w + skin;
+    // (r_i + r_j + skin) * 1.0001 + eps with the staged radii already widened
+    const float base_r = pi.w + skin * 1.0001f + eps;
     // entries of another image (shifted cell or different image counts) keep
     // the minimum image; the home particle is never shifted
     const int32_t img_h = (td.flags & TILE_ALLIMAGE) ? (int32_t)0x7FFFFFFF : simg[oh];
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
               const float ddz = pi.z - q[u].z;
               dsq = __fmaf_rn(ddz, ddz, dsq);
             }
-            const float rc = (base_r + q[u].w) * 1.0001f + eps;
+            const float rc = base_r + q[u].w;
             if (oj < ob && oj != oh && dsq < rc * rc) {
               if (n < cap) out[n * 32] = (int32_t)((uint32_t)sslot[oj] | (simg[oj] != img_h ? 0x80000000u : 0u));
               ++n;
