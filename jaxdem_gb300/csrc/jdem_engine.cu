@@ -289,33 +289,6 @@ int JdemHandle::rebind(const JdemSystemDesc* systems, int n_systems) {
 
 // Grid + cell arrays from the uploaded radii (host copy rad_h) and positions:
 // per-system maximum radius and bounding box, then plan_grid.
-int JdemHandle::plan_cells(const float* rad_h, const float* pos_h) {
-  std::vector<float> rmax((size_t)S, 0.0f), lo((size_t)S * 3, 0.0f), hi((size_t)S * 3, 1.0f);
-  long long off = 0;
-  for (int s = 0; s < S; ++s) {
-    const long long n = desc[s].n;
-    if (n > 0) {
-      for (int a = 0; a < dim; ++a) {
-        lo[(size_t)s * 3 + a] = 3.4e38f;
-        hi[(size_t)s * 3 + a] = -3.4e38f;
-      }
-      for (long long i = off; i < off + n; ++i) {
-        float r = rad_h[i];
-        if (!(r >= 0.0f) || !std::isfinite(r)) return fail(JDEM_ERR_BAD_ARG, "radius must be finite and >= 0");
-        rmax[(size_t)s] = std::max(rmax[(size_t)s], r);
-        for (int a = 0; a < dim; ++a) {
-          float x = pos_h[i * dim + a];
-          if (!std::isfinite(x)) return fail(JDEM_ERR_NONFINITE, "non-finite position in upload");
-          lo[(size_t)s * 3 + a] = std::min(lo[(size_t)s * 3 + a], x - r);
-          hi[(size_t)s * 3 + a] = std::max(hi[(size_t)s * 3 + a], x + r);
-        }
-      }
-    }
-    off += n;
-  }
-  return plan_grid(rmax.data(), lo.data(), hi.data());
-}
-
 // Per-system grids from the maximum radius and (free domain) bounding box,
 // cell arrays sized to fit, then the Verlet-list capacity.
 int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* hi_s) {
@@ -545,30 +518,13 @@ int JdemHandle::reset_ctl() {
 int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
   if (!s || !s->pos_c || !s->rad || !s->mass) return fail(JDEM_ERR_BAD_ARG, "upload: pos_c, rad and mass are required");
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  // the arrays are copied before they are checked: until this upload
+  // succeeds the handle holds no valid state
+  uploaded = false;
   cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   size_t N = (size_t)P;
   int ad = dim == 3 ? 3 : 1;
-  // host copies of radius and positions for grid planning
-  std::vector<float> rad_h(N), pos_h(N * dim);
-  if (N) {
-    if (device_ptrs) {
-      JDEM_CUDA_TRY(this, cudaMemcpy(rad_h.data(), s->rad, N * 4, cudaMemcpyDeviceToHost));
-      JDEM_CUDA_TRY(this, cudaMemcpy(pos_h.data(), s->pos_c, N * dim * 4, cudaMemcpyDeviceToHost));
-    } else {
-      std::memcpy(rad_h.data(), s->rad, N * 4);
-      std::memcpy(pos_h.data(), s->pos_c, N * dim * 4);
-    }
-  }
-  int rc = plan_cells(rad_h.data(), pos_h.data());
-  if (rc) return rc;
-  if (N && s->mat_id) {
-    // material ids index young_eff on the device: validate them here
-    std::vector<int32_t> mat_h(N);
-    if (device_ptrs) JDEM_CUDA_TRY(this, cudaMemcpy(mat_h.data(), s->mat_id, N * 4, cudaMemcpyDeviceToHost));
-    else std::memcpy(mat_h.data(), s->mat_id, N * 4);
-    for (size_t i = 0; i < N; ++i)
-      if (mat_h[i] < 0 || mat_h[i] >= n_mat) return fail(JDEM_ERR_BAD_ARG, "mat_id outside [0, n_materials)");
-  }
+  int rc;
   if (N) {
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_pos, s->pos_c, N * dim * 4, kind, stream));
     if (s->vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_vel, s->vel, N * dim * 4, kind, stream));
@@ -585,49 +541,80 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
       if (!s->bond_id) return fail(JDEM_ERR_BAD_ARG, "upload: bond_id required when bond_width > 0");
       JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_bond, s->bond_id, N * bond_w * 4, kind, stream));
     }
-    // rotational state in caller order
-    std::vector<float> q_h, w_h, t_h, i_h;
-    bool rot_nonzero = false;
-    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, s->q, N * 16, kind, stream));
-    else {
-      q_h.assign(N * 4, 0.0f);
-      for (size_t i = 0; i < N; ++i) q_h[i * 4] = 1.0f;
-      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, q_h.data(), N * 16, cudaMemcpyHostToDevice, stream));
-      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+  }
+  // per-system maximum radius, bounding box and input checks, reduced on the
+  // device (k_scan_input): the host reads eight words per system
+  std::vector<float> rmax((size_t)S, 0.0f), lo((size_t)S * 3, 0.0f), hi((size_t)S * 3, 1.0f);
+  if (N) {
+    if ((long long)S > scan_alloc) {
+      dfree(d_scan);
+      d_scan = nullptr;
+      scan_alloc = 0;
+      if ((rc = dalloc((void**)&d_scan, sizeof(unsigned int) * 8 * (size_t)S))) return rc;
+      scan_alloc = S;
     }
+    std::vector<unsigned int> init((size_t)S * 8, 0u);
+    for (int s2 = 0; s2 < S; ++s2)
+      for (int a = 1; a <= 3; ++a) init[(size_t)s2 * 8 + a] = 0xFFFFFFFFu;
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_scan, init.data(), init.size() * 4, cudaMemcpyHostToDevice, stream));
+    launch_scan_input(dim, P, st_pos, st_rad, s->mat_id ? st_mat : nullptr, n_mat, st_sys, d_scan, stream);
+    JDEM_CUDA_TRY(this, cudaGetLastError());
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(init.data(), d_scan, init.size() * 4, cudaMemcpyDeviceToHost, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    auto dec = [](unsigned int u) {
+      unsigned int v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+      float f;
+      std::memcpy(&f, &v, 4);
+      return f;
+    };
+    for (int s2 = 0; s2 < S; ++s2) {
+      const unsigned int* o8 = init.data() + (size_t)s2 * 8;
+      if (o8[7] & 1u) return fail(JDEM_ERR_BAD_ARG, "radius must be finite and >= 0");
+      if (o8[7] & 2u) return fail(JDEM_ERR_NONFINITE, "non-finite position in upload");
+      if (o8[7] & 4u) return fail(JDEM_ERR_BAD_ARG, "mat_id outside [0, n_materials)");
+      if (desc[s2].n == 0) continue;
+      rmax[(size_t)s2] = dec(o8[0]);
+      for (int a = 0; a < dim; ++a) {
+        lo[(size_t)s2 * 3 + a] = dec(o8[1 + a]);
+        hi[(size_t)s2 * 3 + a] = dec(o8[4 + a]);
+      }
+    }
+  }
+  rc = plan_grid(rmax.data(), lo.data(), hi.data());
+  if (rc) return rc;
+  if (N) {
+    // rotational state in caller order; defaults on the device
+    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, s->q, N * 16, kind, stream));
+    else launch_identity_q((float4*)d_q, (long long)N, stream);
     if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_w, s->ang_vel, N * ad * 4, kind, stream));
     else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
     if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tq, s->torque, N * ad * 4, kind, stream));
     else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
     if (s->inertia) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, s->inertia, N * ad * 4, kind, stream));
-    else {
-      // State.create default: 0.4 m r^2 (3D) / 0.5 m r^2 (2D), state.py:817-823
-      std::vector<float> mass_h(N);
-      if (device_ptrs) JDEM_CUDA_TRY(this, cudaMemcpy(mass_h.data(), s->mass, N * 4, cudaMemcpyDeviceToHost));
-      else std::memcpy(mass_h.data(), s->mass, N * 4);
-      i_h.assign(N * ad, 0.0f);
-      float coeff = dim == 2 ? 0.5f : 0.4f;
-      for (size_t i = 0; i < N; ++i)
-        for (int a = 0; a < ad; ++a) i_h[i * ad + a] = coeff * mass_h[i] * rad_h[i] * rad_h[i];
-      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, i_h.data(), N * ad * 4, cudaMemcpyHostToDevice, stream));
-      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
-    }
+    else launch_default_inertia(dim, (long long)N, st_mass, st_rad, d_inertia, stream);
     // Is any rotational update non-trivial?  With omega = torque = 0 and
     // q = identity every rotation integrator and the reflect renormalisation
     // leave the state bit-identical, so the rotation kernel can be skipped.
-    {
-      std::vector<float> qq(N * 4), ww(N * ad), tt(N * ad);
-      if (device_ptrs || !s->q) JDEM_CUDA_TRY(this, cudaMemcpy(qq.data(), d_q, N * 16, cudaMemcpyDeviceToHost));
-      else std::memcpy(qq.data(), s->q, N * 16);
-      JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
-      JDEM_CUDA_TRY(this, cudaMemcpy(ww.data(), d_w, N * ad * 4, cudaMemcpyDeviceToHost));
-      JDEM_CUDA_TRY(this, cudaMemcpy(tt.data(), d_tq, N * ad * 4, cudaMemcpyDeviceToHost));
-      for (size_t i = 0; i < N && !rot_nonzero; ++i) {
-        if (qq[i * 4] != 1.0f || qq[i * 4 + 1] != 0.0f || qq[i * 4 + 2] != 0.0f || qq[i * 4 + 3] != 0.0f)
-          rot_nonzero = true;
-        for (int a = 0; a < ad; ++a)
-          if (ww[i * ad + a] != 0.0f || tt[i * ad + a] != 0.0f) rot_nonzero = true;
-      }
+    // Arrays the caller did not pass hold exactly those defaults.
+    bool rot_nonzero = false;
+    auto host_view = [&](const float* src, size_t count, std::vector<float>& tmp) -> const float* {
+      if (!device_ptrs) return src;
+      tmp.resize(count);
+      if (cudaMemcpy(tmp.data(), src, count * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return nullptr;
+      return tmp.data();
+    };
+    std::vector<float> tmp;
+    if (s->q) {
+      const float* q = host_view(s->q, N * 4, tmp);
+      if (!q) return fail(JDEM_ERR_CUDA, "upload: reading q");
+      for (size_t i = 0; i < N && !rot_nonzero; ++i)
+        rot_nonzero = q[i * 4] != 1.0f || q[i * 4 + 1] != 0.0f || q[i * 4 + 2] != 0.0f || q[i * 4 + 3] != 0.0f;
+    }
+    for (const float* src : {s->ang_vel, s->torque}) {
+      if (!src || rot_nonzero) continue;
+      const float* v = host_view(src, N * ad, tmp);
+      if (!v) return fail(JDEM_ERR_CUDA, "upload: reading rotational state");
+      for (size_t i = 0; i < N * ad && !rot_nonzero; ++i) rot_nonzero = v[i] != 0.0f;
     }
     rot_active = rot_nonzero;
     launch_pack(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, st_mat, st_fixed, st_sys, stream);

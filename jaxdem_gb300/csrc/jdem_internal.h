@@ -22,6 +22,8 @@ struct JdemHandle {
   std::vector<jdem::TileDesc> tiles_h;
   jdem::TileDesc* d_tiles = nullptr;
   long long tiles_alloc = 0;
+  unsigned int* d_scan = nullptr;  // per-system upload summary (k_scan_input)
+  long long scan_alloc = 0;
   float skin = 0.0f;
   int chunk = 50;
   int n_mat = 1;
@@ -76,7 +78,6 @@ struct JdemHandle {
   int ensure_capacity(long long p_need, int s_need);
   int bind_systems();
   int rebind(const JdemSystemDesc* systems, int n_systems);
-  int plan_cells(const float* rad_h, const float* pos_h);
   int plan_grid(const float* rmax_s, const float* lo_s, const float* hi_s);
   int upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
                       const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s);

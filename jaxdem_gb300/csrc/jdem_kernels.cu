@@ -833,6 +833,83 @@ void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, con
   else k_pack<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc, rad, mass, mat, fixed, sys_of);
 }
 
+// Per-system summary of uploaded particle arrays for grid planning, so the
+// host reads a few words per system instead of scanning every particle:
+// out[8 s] = max radius, out[8 s + 1..3] = min (x - r), out[8 s + 4..6] =
+// max (x + r) (order-preserving uints), out[8 s + 7] = flags (1: radius not
+// finite or negative, 2: non-finite position, 4: material id out of range).
+// A warp whose particles share one system reduces with shuffles first.
+template <int DIM>
+__global__ void k_scan_input(long long N, const float* __restrict__ pos, const float* __restrict__ rad,
+                             const int32_t* __restrict__ mat, int n_mat, const int32_t* __restrict__ sys_of,
+                             unsigned int* __restrict__ out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool valid = i < N;
+  const int s = valid ? sys_of[i] : -1;
+  float r = 0.0f, lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  unsigned int flags = 0u;
+  if (valid) {
+    r = rad[i];
+    if (!(r >= 0.0f) || !isfinite(r)) flags |= 1u;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      const float x = pos[i * DIM + a];
+      if (!isfinite(x)) flags |= 2u;
+      lo[a] = x - r;
+      hi[a] = x + r;
+    }
+    if (mat && (mat[i] < 0 || mat[i] >= n_mat)) flags |= 4u;
+    if (!(r >= 0.0f)) r = 0.0f;
+  }
+  const int s0 = __shfl_sync(0xffffffffu, s, 0);
+  if (__all_sync(0xffffffffu, s == s0 || s < 0) && s0 >= 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+      flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+        hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+      }
+    }
+    if ((threadIdx.x & 31) != 0) return;
+  } else if (!valid) {
+    return;
+  }
+  unsigned int* o8 = out + 8 * (long long)(s >= 0 ? s : s0);
+  atomicMax(&o8[0], f2ord(r));
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    atomicMin(&o8[1 + a], f2ord(lo[a]));
+    atomicMax(&o8[4 + a], f2ord(hi[a]));
+  }
+  if (flags) atomicOr(&o8[7], flags);
+}
+
+// State.create's default moment of inertia, 0.4 m r^2 (3D) / 0.5 m r^2 (2D)
+// (state.py:817-823), per particle in caller order.
+__global__ void k_default_inertia(long long N, int ad, float coeff, const float* __restrict__ mass,
+                                  const float* __restrict__ rad, float* __restrict__ inertia) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float v = coeff * mass[i] * rad[i] * rad[i];
+  for (int a = 0; a < ad; ++a) inertia[i * ad + a] = v;
+}
+
+void launch_scan_input(int dim, long long N, const float* pos, const float* rad, const int32_t* mat, int n_mat,
+                       const int32_t* sys_of, unsigned int* out, cudaStream_t st) {
+  if (N <= 0) return;
+  if (dim == 3) k_scan_input<3><<<nblk(N, 256), 256, 0, st>>>(N, pos, rad, mat, n_mat, sys_of, out);
+  else k_scan_input<2><<<nblk(N, 256), 256, 0, st>>>(N, pos, rad, mat, n_mat, sys_of, out);
+}
+
+void launch_default_inertia(int dim, long long N, const float* mass, const float* rad, float* inertia,
+                            cudaStream_t st) {
+  if (N <= 0) return;
+  k_default_inertia<<<nblk(N, 256), 256, 0, st>>>(N, dim == 3 ? 3 : 1, dim == 2 ? 0.5f : 0.4f, mass, rad, inertia);
+}
+
 __global__ void k_identity_q(float4* q, long long n) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) q[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);

@@ -9,6 +9,10 @@ void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, con
                  const int32_t* sys_of, cudaStream_t st);
 void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st);
 void launch_identity_q(float4* q, long long n, cudaStream_t st);
+void launch_scan_input(int dim, long long N, const float* pos, const float* rad, const int32_t* mat, int n_mat,
+                       const int32_t* sys_of, unsigned int* out, cudaStream_t st);
+void launch_default_inertia(int dim, long long N, const float* mass, const float* rad, float* inertia,
+                            cudaStream_t st);
 void launch_segcopy(const long long* seg, int nseg, int narr, const float* const* src, float* const* dst,
                     const int* width, cudaStream_t st);
 void launch_scan(const Bufs& b, cudaStream_t st);

@@ -387,3 +387,42 @@ def test_clustered_particles_overflow_paths():
     assert st["list_tiles"] > 0
     assert force_err(f0, ref) <= 1e-5
     assert min_image_diff(out["pos_c"], _oracle_rollout(w, ref), w.box_size) <= 1e-4
+
+
+def test_upload_rejects_bad_input_and_recovers():
+    """Non-finite positions, negative radii and material ids outside the table are
+    rejected at upload (checked on the device); the handle then holds no state until
+    an upload succeeds."""
+    from jaxdem_gb300._lib import JdemError
+
+    w = small_periodic(N=1024)
+    eng = make_engine(w)
+    try:
+        bad = w.pos.copy()
+        bad[17, 1] = np.nan
+        with pytest.raises(JdemError) as e:
+            eng.upload(pos=bad, rad=w.rad, mass=w.mass, vel=w.vel)
+        assert "non-finite" in str(e.value)
+        with pytest.raises(JdemError):
+            eng.step(1)
+        rad = w.rad.copy()
+        rad[3] = -0.5
+        with pytest.raises(JdemError):
+            eng.upload(pos=w.pos, rad=rad, mass=w.mass, vel=w.vel)
+        mat = np.zeros(w.N, np.int32)
+        mat[5] = 7
+        with pytest.raises(JdemError):
+            eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat)
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+        eng.step(10)
+        out = eng.download()
+    finally:
+        eng.close()
+    ref = make_engine(w)
+    try:
+        ref.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+        ref.step(10)
+        want = ref.download()
+    finally:
+        ref.close()
+    assert np.array_equal(out["pos_c"], want["pos_c"])
