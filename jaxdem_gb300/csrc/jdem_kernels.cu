@@ -840,10 +840,15 @@ void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, con
 // finite or negative, 2: non-finite position, 4: material id out of range).
 // A warp whose particles share one system reduces with shuffles first.
 template <int DIM>
-__global__ void k_scan_input(long long N, const float* __restrict__ pos, const float* __restrict__ rad,
-                             const int32_t* __restrict__ mat, int n_mat, const int32_t* __restrict__ sys_of,
-                             unsigned int* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_scan_input(long long N, const float* __restrict__ pos,
+                                                    const float* __restrict__ rad, const int32_t* __restrict__ mat,
+                                                    int n_mat, const int32_t* __restrict__ sys_of,
+                                                    unsigned int* __restrict__ out) {
+  __shared__ int w_sys[8];
+  __shared__ float w_val[8][7];
+  __shared__ unsigned int w_flag[8];
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const bool valid = i < N;
   const int s = valid ? sys_of[i] : -1;
   float r = 0.0f, lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
@@ -861,8 +866,11 @@ __global__ void k_scan_input(long long N, const float* __restrict__ pos, const f
     if (mat && (mat[i] < 0 || mat[i] >= n_mat)) flags |= 4u;
     if (!(r >= 0.0f)) r = 0.0f;
   }
+  // one system per warp: shuffle reduction, then one record per warp in
+  // shared memory; mixed warps (a system boundary) use per-lane atomics
   const int s0 = __shfl_sync(0xffffffffu, s, 0);
-  if (__all_sync(0xffffffffu, s == s0 || s < 0) && s0 >= 0) {
+  const bool uniform = __all_sync(0xffffffffu, s == s0 || s < 0) && s0 >= 0;
+  if (uniform) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
@@ -873,18 +881,56 @@ __global__ void k_scan_input(long long N, const float* __restrict__ pos, const f
         hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
       }
     }
-    if ((threadIdx.x & 31) != 0) return;
-  } else if (!valid) {
-    return;
-  }
-  unsigned int* o8 = out + 8 * (long long)(s >= 0 ? s : s0);
-  atomicMax(&o8[0], f2ord(r));
+  } else if (valid) {
+    unsigned int* o8 = out + 8 * (long long)s;
+    atomicMax(&o8[0], f2ord(r));
 #pragma unroll
-  for (int a = 0; a < DIM; ++a) {
-    atomicMin(&o8[1 + a], f2ord(lo[a]));
-    atomicMax(&o8[4 + a], f2ord(hi[a]));
+    for (int a = 0; a < DIM; ++a) {
+      atomicMin(&o8[1 + a], f2ord(lo[a]));
+      atomicMax(&o8[4 + a], f2ord(hi[a]));
+    }
+    if (flags) atomicOr(&o8[7], flags);
   }
-  if (flags) atomicOr(&o8[7], flags);
+  if (lane == 0) {
+    w_sys[wid] = uniform ? s0 : -1;
+    w_val[wid][0] = r;
+    for (int a = 0; a < 3; ++a) {
+      w_val[wid][1 + a] = lo[a];
+      w_val[wid][4 + a] = hi[a];
+    }
+    w_flag[wid] = flags;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  // merge consecutive warps of one system; one set of atomics per run
+  const int nw = blockDim.x >> 5;
+  for (int w = 0; w < nw;) {
+    const int sw = w_sys[w];
+    if (sw < 0) {
+      ++w;
+      continue;
+    }
+    float v[7];
+    for (int k = 0; k < 7; ++k) v[k] = w_val[w][k];
+    unsigned int f = w_flag[w];
+    int e = w + 1;
+    for (; e < nw && w_sys[e] == sw; ++e) {
+      v[0] = fmaxf(v[0], w_val[e][0]);
+      for (int a = 0; a < 3; ++a) {
+        v[1 + a] = fminf(v[1 + a], w_val[e][1 + a]);
+        v[4 + a] = fmaxf(v[4 + a], w_val[e][4 + a]);
+      }
+      f |= w_flag[e];
+    }
+    unsigned int* o8 = out + 8 * (long long)sw;
+    atomicMax(&o8[0], f2ord(v[0]));
+    for (int a = 0; a < DIM; ++a) {
+      atomicMin(&o8[1 + a], f2ord(v[1 + a]));
+      atomicMax(&o8[4 + a], f2ord(v[4 + a]));
+    }
+    if (f) atomicOr(&o8[7], f);
+    w = e;
+  }
 }
 
 // State.create's default moment of inertia, 0.4 m r^2 (3D) / 0.5 m r^2 (2D)
