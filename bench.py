@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     p.add_argument("--no-batched", action="store_true", help="skip the batched mixed-size summary")
     p.add_argument("--no-served", action="store_true", help="skip the serving summary")
+    p.add_argument("--no-rollout", action="store_true", help="skip the trajectory-streaming summary")
+    p.add_argument("--frame-stride", type=int, default=10, help="steps between saved rollout frames")
     p.add_argument("--serve-requests", type=int, default=120, help="prefix of the request stream served")
     p.add_argument("--serve-baseline", type=int, default=16, help="requests served one at a time (baseline)")
     p.add_argument("--no-tune", action="store_true", help="skip the skin autotuner")
@@ -326,12 +328,53 @@ def run_ours(args, rank, world, dist):
         "clocks": clk,
     }
     eng.close()
+    if rank == 0 and world == 1 and not args.no_rollout:
+        line["rollout"] = run_rollout(args, w, young, skin, dev, torch)
     if rank == 0 and world == 1 and not args.no_batched:
         line["batched"] = run_batched(args, dev, flush, torch)
     if rank == 0 and world == 1 and not args.no_served:
         line["served"] = run_served(args, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_rollout(args, w, young, skin, dev, torch):
+    """System.trajectory_rollout through jdem_rollout: the timed steps with a frame
+    (pos_c, vel, force in caller order) saved every ``--frame-stride`` steps, into
+    device memory and into fresh pageable host arrays, beside the same steps
+    without frames.  Wall-clock per call, best of three."""
+    from jaxdem_gb300._lib import Engine
+
+    K, k = args.steps, max(1, args.frame_stride)
+    T = max(1, K // k)
+    strides = np.full(T, k, np.int64)
+    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
+    fields = ("pos_c", "vel", "force")
+    dev_out = {f: torch.empty((T, w.N, w.dim), dtype=torch.float32, device=f"cuda:{dev}") for f in fields}
+
+    def best(fn):
+        t = []
+        for _ in range(3):
+            eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+            eng.step(CHUNK)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            t.append(time.perf_counter() - t0)
+        return min(t)
+
+    eng.rollout(strides[:2], fields=fields, boxes=False)  # graphs for the stride, ring allocation
+    plain = best(lambda: eng.step(T * k))
+    on_dev = best(lambda: eng.rollout(strides, fields=fields, out=dev_out, boxes=False))
+    on_host = best(lambda: eng.rollout(strides, fields=fields, boxes=False))
+    eng.close()
+    frame_bytes = 3 * w.N * w.dim * 4
+    rate = lambda s: w.N * T * k / s
+    return {"frames": T, "frame_stride": k, "frame_bytes": frame_bytes,
+            "plain_steps": rate(plain), "to_device": rate(on_dev), "to_host_pageable": rate(on_host),
+            "unit": "particle-steps/s",
+            "host_frame_GBps": frame_bytes * T / on_host / 1e9,
+            "note": "wall clock per call (best of 3); host arrays freshly allocated each call"}
 
 
 def run_batched(args, dev, flush, torch, n_systems=4096, steps=1000):

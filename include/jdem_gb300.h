@@ -160,6 +160,35 @@ int jdem_step_timed(JdemHandle* h, int64_t n, double* total_ms, double* force_ms
 int jdem_download(JdemHandle* h, JdemHostState* host);
 int jdem_download_device(JdemHandle* h, JdemHostState* dev);
 
+/* Destinations of jdem_rollout, stacked along a leading frame axis T in the
+ * reference's particle order; a NULL pointer skips that field.
+ *   pos_c, vel, force  (T, N, dim)      q  (T, N, 4)
+ *   ang_vel, torque    (T, N, 1|3)
+ *   box, anchor        (T, n_systems, 3): Domain.box_size / anchor after the
+ *                      frame's steps (unused axes 0), always host memory. */
+typedef struct {
+  float* pos_c;
+  float* vel;
+  float* force;
+  float* q;
+  float* ang_vel;
+  float* torque;
+  float* box;
+  float* anchor;
+  int32_t device_ptrs; /* 1: the particle fields are device memory (frames stay in HBM) */
+  int32_t ring;        /* host particle fields: device frame slots in flight (0: 3) */
+} JdemFrames;
+
+/* System.trajectory_rollout (system.py:606-699; scan body _trajectory_rollout,
+ * system.py:99-120) with the default save_fn: for t in [0, n_frames), run
+ * strides[t] steps (System.step), then save frame t -- a stride of 0 saves the
+ * current state again.  Host destinations are filled from a ring of device
+ * frame slots by a second stream whose copies overlap the next frame's steps
+ * (fully for page-locked destinations -- cudaHostAlloc / jdem_host_register;
+ * a pageable destination makes each frame's copy return only once it has
+ * landed).  Blocks until every frame has landed. */
+int jdem_rollout(JdemHandle* h, const int64_t* strides, int64_t n_frames, const JdemFrames* out);
+
 /* DynamicCellList.compute_force (cell_list.py:434-464): contact forces at the
  * current positions (no gravity, no integration); torque = 0 for spheres.
  * Results are read with jdem_download. */

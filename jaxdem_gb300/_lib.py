@@ -93,6 +93,21 @@ class HostState(C.Structure):
     ]
 
 
+class Frames(C.Structure):
+    _fields_ = [
+        ("pos_c", C.c_void_p),
+        ("vel", C.c_void_p),
+        ("force", C.c_void_p),
+        ("q", C.c_void_p),
+        ("ang_vel", C.c_void_p),
+        ("torque", C.c_void_p),
+        ("box", C.c_void_p),
+        ("anchor", C.c_void_p),
+        ("device_ptrs", C.c_int32),
+        ("ring", C.c_int32),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("n_particles", C.c_int64),
@@ -127,6 +142,7 @@ _PROTOS = [
     ("jdem_step_timed", [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
     ("jdem_download", [C.c_void_p, C.POINTER(HostState)], C.c_int),
     ("jdem_download_device", [C.c_void_p, C.POINTER(HostState)], C.c_int),
+    ("jdem_rollout", [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(Frames)], C.c_int),
     ("jdem_compute_force", [C.c_void_p], C.c_int),
     ("jdem_energy", [C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     ("jdem_energy_per_system", [C.c_void_p, C.POINTER(C.c_double)], C.c_int),
@@ -296,6 +312,54 @@ class Engine:
                 assert out[k].flags["C_CONTIGUOUS"] and out[k].dtype == np.float32
                 setattr(hs, k, out[k].ctypes.data)
         self._check(self.lib.jdem_download(self.h, C.byref(hs)))
+        return out
+
+    FRAME_FIELDS = ("pos_c", "vel", "force", "q", "ang_vel", "torque")
+
+    def rollout(self, strides, fields=("pos_c", "vel", "force", "q", "ang_vel", "torque"), out=None,
+                ring: int = 0, boxes: bool = True) -> dict:
+        """Run ``strides[t]`` steps per frame and save the selected fields after each
+        (``jdem_rollout``).  Returns arrays of shape ``(T, P, ...)`` in caller order, plus
+        ``box`` / ``anchor`` of shape ``(T, S, dim)`` when ``boxes``.
+
+        ``out`` may hold preallocated destinations: numpy arrays (page-locked ones are
+        written by the copy engine directly) or CUDA tensors exposing ``data_ptr()``
+        (then every particle field must be a CUDA tensor and frames stay in HBM)."""
+        st = np.ascontiguousarray(np.asarray(strides, np.int64).reshape(-1))
+        T, P, d = len(st), self.P, self.dim
+        ad = 3 if d == 3 else 1
+        tails = {"pos_c": (d,), "vel": (d,), "force": (d,), "q": (4,), "ang_vel": (ad,), "torque": (ad,)}
+        for k in fields:
+            if k not in tails:
+                raise ValueError(f"unknown frame field {k!r}")
+        out = dict(out or {})
+        fr = Frames()
+        device = None
+        for k in fields:
+            a = out.get(k)
+            if a is None:
+                a = out[k] = np.empty((T, P, *tails[k]), np.float32)
+            if hasattr(a, "data_ptr"):
+                if tuple(a.shape) != (T, P, *tails[k]) or not a.is_contiguous() or str(a.dtype) != "torch.float32":
+                    raise ValueError(f"frame field {k}: expected contiguous float32 {(T, P, *tails[k])}")
+                dev, ptr = True, a.data_ptr()
+            else:
+                if a.shape != (T, P, *tails[k]) or not a.flags["C_CONTIGUOUS"] or a.dtype != np.float32:
+                    raise ValueError(f"frame field {k}: expected contiguous float32 {(T, P, *tails[k])}")
+                dev, ptr = False, a.ctypes.data
+            if device is not None and dev != device:
+                raise ValueError("frame fields must be all host arrays or all device tensors")
+            device = dev
+            setattr(fr, k, ptr if a.size else None)
+        fr.device_ptrs = 1 if device else 0
+        fr.ring = int(ring)
+        if boxes:
+            out["box"] = np.zeros((T, self.S, 3), np.float32)
+            out["anchor"] = np.zeros((T, self.S, 3), np.float32)
+            fr.box, fr.anchor = out["box"].ctypes.data, out["anchor"].ctypes.data
+        self._check(self.lib.jdem_rollout(self.h, st.ctypes.data if T else None, T, C.byref(fr)))
+        if boxes:
+            out["box"], out["anchor"] = out["box"][..., :d], out["anchor"][..., :d]
         return out
 
     # -- work -------------------------------------------------------------

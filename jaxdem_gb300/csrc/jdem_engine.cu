@@ -29,21 +29,13 @@ const char* kStatusNames[] = {"ok",          "bad argument", "capacity overflow"
 
 // ------------------------------------------------------------------ helpers
 
-#define JDEM_CUDA_TRY(h, expr)                                                          \
-  do {                                                                                  \
-    cudaError_t _e = (expr);                                                            \
-    if (_e != cudaSuccess) {                                                            \
-      return (h)->fail(_e == cudaErrorMemoryAllocation ? JDEM_ERR_OOM : JDEM_ERR_CUDA,   \
-                       std::string(#expr) + ": " + cudaGetErrorString(_e));            \
-    }                                                                                   \
-  } while (0)
-
 int JdemHandle::fail(int code, const std::string& msg) {
   err = msg;
   return code;
 }
 
 void JdemHandle::free_all() {
+  free_frames();
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
   graphs.clear();
   for (void* p : allocs) cudaFree(p);
@@ -793,18 +785,7 @@ int JdemHandle::step_async(long long n) {
   }
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
   int bbox = any_free ? MODE_BBOX : 0;
-  if (any_free) {
-    // ordered-int encodings of +inf (min slots) and -inf (max slots)
-    std::vector<unsigned int> init((size_t)S * 6);
-    for (int s = 0; s < S; ++s)
-      for (int a = 0; a < 3; ++a) {
-        init[s * 6 + a] = 0xFFFFFFFFu;
-        init[s * 6 + 3 + a] = 0u;
-      }
-    JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.bbox, init.data(), sizeof(unsigned int) * S * 6,
-                                        cudaMemcpyHostToDevice, stream));
-    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
-  }
+  if (any_free) launch_bbox_reset(b, stream);  // stream-ordered: no host round trip
   launch_pre(dim, b, n == 1 ? bbox : 0, stream);
   JDEM_CUDA_TRY(this, cudaGetLastError());
   // steps 1 .. n-1 run MODE_STEP (their epilogue starts the next step);

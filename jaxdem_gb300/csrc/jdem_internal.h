@@ -7,6 +7,17 @@
 #include "../../include/jdem_gb300.h"
 #include "jdem_device.cuh"
 
+// Run a CUDA call; on failure record the message on the handle and return
+// JDEM_ERR_OOM / JDEM_ERR_CUDA from the enclosing member function.
+#define JDEM_CUDA_TRY(h, expr)                                                          \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess) {                                                            \
+      return (h)->fail(_e == cudaErrorMemoryAllocation ? JDEM_ERR_OOM : JDEM_ERR_CUDA,   \
+                       std::string(#expr) + ": " + cudaGetErrorString(_e));            \
+    }                                                                                   \
+  } while (0)
+
 struct JdemHandle {
   // configuration
   int dev = 0;
@@ -49,6 +60,13 @@ struct JdemHandle {
   uint8_t* st_fixed = nullptr;
   float4* d_q4 = nullptr;
   float *d_q = nullptr, *d_w = nullptr, *d_tq = nullptr, *d_inertia = nullptr;
+
+  // trajectory frames (jdem_rollout): device slot ring and the copy stream
+  // that drains it
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> ev_frame;  // per slot: unpacked, copied
+  char* d_frames = nullptr;
+  size_t d_frames_bytes = 0;
 
   // runtime
   cudaStream_t stream = nullptr;
@@ -98,4 +116,6 @@ struct JdemHandle {
   int contacts(int32_t* pairs, long long cap, long long* count);
   int neighbor_list(float cutoff, int max_neighbors, int32_t* out, int32_t* overflow);
   int domain_state(float* box, float* anchor);
+  int rollout(const int64_t* strides, long long n_frames, const JdemFrames* out);
+  void free_frames();
 };

@@ -78,18 +78,32 @@ __global__ void k_unpack(Bufs b, float* __restrict__ pos, float* __restrict__ ve
   if (t >= b.P) return;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   long long i = b.orig[sel][t];
-  float4 p = b.pos[ps][t], v = b.vel[sel][t], f = b.frc[sel][t];
-  pos[i * DIM + 0] = p.x;
-  pos[i * DIM + 1] = p.y;
-  vel[i * DIM + 0] = v.x;
-  vel[i * DIM + 1] = v.y;
-  frc[i * DIM + 0] = f.x;
-  frc[i * DIM + 1] = f.y;
-  if (DIM == 3) {
-    pos[i * DIM + 2] = p.z;
-    vel[i * DIM + 2] = v.z;
-    frc[i * DIM + 2] = f.z;
+  // a null destination skips that field (trajectory frames select fields)
+  if (pos) {
+    float4 p = b.pos[ps][t];
+    pos[i * DIM + 0] = p.x;
+    pos[i * DIM + 1] = p.y;
+    if (DIM == 3) pos[i * DIM + 2] = p.z;
   }
+  if (vel) {
+    float4 v = b.vel[sel][t];
+    vel[i * DIM + 0] = v.x;
+    vel[i * DIM + 1] = v.y;
+    if (DIM == 3) vel[i * DIM + 2] = v.z;
+  }
+  if (frc) {
+    float4 f = b.frc[sel][t];
+    frc[i * DIM + 0] = f.x;
+    frc[i * DIM + 1] = f.y;
+    if (DIM == 3) frc[i * DIM + 2] = f.z;
+  }
+}
+
+// Free-domain bounding box accumulators: ordered-int +inf in the min words,
+// -inf in the max words of every system.
+__global__ void k_bbox_reset(unsigned int* __restrict__ bb, int S) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < S * 6) bb[k] = (k % 6) < 3 ? 0xFFFFFFFFu : 0u;
 }
 
 // --------------------------------------------------------------- re-binning
@@ -992,6 +1006,11 @@ void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, c
   if (b.P == 0) return;
   if (dim == 3) k_unpack<3><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc);
   else k_unpack<2><<<nblk(b.P, 256), 256, 0, st>>>(b, pos, vel, frc);
+}
+
+void launch_bbox_reset(const Bufs& b, cudaStream_t st) {
+  if (b.S == 0) return;
+  k_bbox_reset<<<(unsigned)((b.S * 6 + 255) / 256), 256, 0, st>>>((unsigned int*)b.bbox, b.S);
 }
 
 void launch_scan(const Bufs& b, cudaStream_t st) {

@@ -7,7 +7,9 @@ namespace jdem {
 void launch_pack(int dim, const Bufs& b, const float* pos, const float* vel, const float* frc,
                  const float* rad, const float* mass, const int32_t* mat, const uint8_t* fixed,
                  const int32_t* sys_of, cudaStream_t st);
+// Slot order -> caller order; a null destination skips that field.
 void launch_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, cudaStream_t st);
+void launch_bbox_reset(const Bufs& b, cudaStream_t st);
 void launch_identity_q(float4* q, long long n, cudaStream_t st);
 void launch_scan_input(int dim, long long N, const float* pos, const float* rad, const int32_t* mat, int n_mat,
                        const int32_t* sys_of, unsigned int* out, cudaStream_t st);

@@ -208,25 +208,119 @@ def step(state: State, system, n: int):
     return download(eng, state), _advance_system(system, eng, n, state.batch_size > 1 and state.pos_c.ndim == 3)
 
 
-def rollout(state: State, system, strides: np.ndarray, save_fn: Callable):
-    from .system import System
+def _rotation_static(state: State) -> bool:
+    """Identity orientations with zero angular velocity and torque: the engine leaves
+    q, ang_vel and torque untouched (the spiral integrators keep them fixed)."""
+    q = state.q
+    return (bool(np.all(q.w == 1)) and not np.any(q.xyz) and not np.any(state.ang_vel)
+            and not np.any(state.torque))
 
+
+def _frame_times(system, strides: np.ndarray, batched: bool):
+    """Per-frame ``time`` and ``step_count`` (float32 ``time += dt`` per step,
+    system.py:62-66), accumulated in float32 step by step."""
+    dt = np.asarray(system.dt, F32)
+    t0 = np.asarray(system.time, F32)
+    total = int(strides.sum())
+    steps = np.cumsum(strides)
+    if total:
+        inc = np.broadcast_to(dt, (total, *dt.shape))
+        acc = np.cumsum(np.concatenate([t0[None], inc], 0), axis=0, dtype=F32)
+        times = acc[steps]
+    else:
+        times = np.broadcast_to(t0, (len(strides), *t0.shape)).copy()
+    counts = (np.asarray(system.step_count)[None] + steps.reshape((-1,) + (1,) * np.ndim(system.step_count)))
+    return times.astype(F32), counts.astype(np.int32)
+
+
+def rollout(state: State, system, strides: np.ndarray, save_fn: Callable):
+    """``System.trajectory_rollout`` on the device: frames are unpacked into a device
+    ring after their strides and streamed to the host on a copy stream while the
+    next stride runs (``jdem_rollout``)."""
+    from .system import _save_state_system
+
+    strides = np.asarray(strides, np.int64).reshape(-1)
+    if np.any(strides < 0):
+        raise ValueError("strides must be >= 0")
+    T = len(strides)
     eng = engine_for(state, system)
     upload(eng, state)
-    frames = []
-    st, sy = state, system
     batched = state.batch_size > 1 and state.pos_c.ndim == 3
-    for k in strides:
-        k = int(k)
-        if k < 0:
-            raise ValueError("strides must be >= 0")
-        if k > 0:
-            eng.step(k)
-            st = download(eng, state)
-            sy = _advance_system(sy, eng, k, batched)
-        frames.append(save_fn(st, sy))
-    traj = _stack_frames(frames)
-    return st, sy, traj
+    rot_static = _rotation_static(state)
+    fields = ("pos_c", "vel", "force") if rot_static else Engine.FRAME_FIELDS
+    free = system.domain.type_name == "free"
+    fr = eng.rollout(strides, fields=fields, boxes=free)
+    shp = state.pos_c.shape
+    frames = {k: fr[k].reshape((T, *shp)) for k in ("pos_c", "vel", "force")}
+    if rot_static:
+        qa = state.q.as_array()
+        frames["q"] = np.broadcast_to(qa, (T, *qa.shape))
+        frames["ang_vel"] = np.broadcast_to(state.ang_vel, (T, *state.ang_vel.shape))
+        frames["torque"] = np.broadcast_to(state.torque, (T, *state.torque.shape))
+    else:
+        frames["q"] = fr["q"].reshape((T, *shp[:-1], 4))
+        frames["ang_vel"] = fr["ang_vel"].reshape((T, *state.ang_vel.shape))
+        frames["torque"] = fr["torque"].reshape((T, *state.torque.shape))
+    times, counts = _frame_times(system, strides, batched)
+    boxes = anchors = None
+    if free:
+        boxes, anchors = fr["box"], fr["anchor"]
+        if not batched:
+            boxes, anchors = boxes[:, 0], anchors[:, 0]
+
+    def frame_system(t: int):
+        sy = dataclasses.replace(system, time=times[t] if times[t].ndim else F32(times[t]),
+                                 step_count=counts[t] if counts[t].ndim else np.int32(counts[t]))
+        if free:
+            box = boxes[t].astype(F32)
+            sy = dataclasses.replace(sy, domain=dataclasses.replace(
+                system.domain, box_size=box, anchor=anchors[t].astype(F32), inv_box_size=(F32(1.0) / box).astype(F32)))
+        return sy
+
+    def frame_state(t: int, copy: bool = False) -> State:
+        pick = (lambda a: np.array(a[t])) if copy else (lambda a: a[t])
+        st = dataclasses.replace(state, pos_c=pick(frames["pos_c"]), vel=pick(frames["vel"]),
+                                 force=pick(frames["force"]), q=Quaternion.from_array(frames["q"][t]),
+                                 ang_vel=pick(frames["ang_vel"]), torque=pick(frames["torque"]))
+        return st
+
+    if T == 0:
+        # a scan of length 0: every saved leaf gets an empty leading frame axis
+        return state, system, _empty_frames(_stack_frames([save_fn(state, system)]))
+    final_state, final_system = frame_state(T - 1, copy=True), frame_system(T - 1)
+    if save_fn is _save_state_system:
+        # the default save_fn stacks (state, system): build the stacked pytrees
+        # from the frame arrays; static fields are read-only broadcasts
+        kw = {}
+        for f in dataclasses.fields(state):
+            v = getattr(state, f.name)
+            if f.name in frames and f.name != "q":
+                kw[f.name] = frames[f.name]
+            elif f.name == "q":
+                qa = frames["q"]
+                kw[f.name] = Quaternion(qa[..., 0:1], qa[..., 1:])
+            else:
+                kw[f.name] = np.broadcast_to(v, (T, *np.shape(v)))
+        traj = (State(**kw), _stack_frames([frame_system(t) for t in range(T)]))
+        return final_state, final_system, traj
+    return final_state, final_system, _stack_frames([save_fn(frame_state(t), frame_system(t)) for t in range(T)])
+
+
+def _empty_frames(tree):
+    if isinstance(tree, tuple):
+        return tuple(_empty_frames(x) for x in tree)
+    if isinstance(tree, Quaternion):
+        return Quaternion(tree.w[:0], tree.xyz[:0])
+    if dataclasses.is_dataclass(tree):
+        kw = {}
+        for f in dataclasses.fields(tree):
+            v = getattr(tree, f.name)
+            kw[f.name] = _empty_frames(v) if isinstance(v, (np.ndarray, tuple, Quaternion)) or (
+                dataclasses.is_dataclass(v) and not callable(v)) else v
+        return dataclasses.replace(tree, **kw)
+    if isinstance(tree, np.ndarray):
+        return tree[:0]
+    return tree
 
 
 def _stack_frames(frames):

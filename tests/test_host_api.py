@@ -117,6 +117,45 @@ def test_trajectory_rollout_argument_checks():
         jdem.System.trajectory_rollout(st, sy, strides=np.ones((2, 2), int))
 
 
+def test_rollout_frame_times_match_stepwise_float32():
+    """Frame times of a rollout: float32 ``time += dt`` once per step (system.py:62-66),
+    for a scalar system and for a batch with per-member dt and time."""
+    from jaxdem_gb300 import session
+
+    strides = np.array([0, 3, 7, 0, 5, 1], np.int64)
+    st = jdem.State.create(pos=np.zeros((2, 3)))
+    sy = jdem.System.create(state=st, dt=1e-3, time=0.1)
+    times, counts = session._frame_times(sy, strides, batched=False)
+    t, ref = F32(0.1), []
+    for k in strides:
+        for _ in range(k):
+            t = F32(t + F32(1e-3))
+        ref.append(t)
+    assert times.dtype == F32 and np.array_equal(times, ref)
+    assert np.array_equal(counts, np.cumsum(strides))
+    bsy = jdem.System.stack([jdem.System.create(state=st, dt=dt, time=t0) for dt, t0 in ((1e-3, 0.0), (3e-4, 2.0))])
+    times, counts = session._frame_times(bsy, strides, batched=True)
+    assert times.shape == (len(strides), 2) and counts.shape == (len(strides), 2)
+    for b, (dt, t0) in enumerate(((1e-3, 0.0), (3e-4, 2.0))):
+        t, ref = F32(t0), []
+        for k in strides:
+            for _ in range(k):
+                t = F32(t + F32(dt))
+            ref.append(t)
+        assert np.array_equal(times[:, b], ref)
+
+
+def test_empty_rollout_frames_have_a_zero_frame_axis():
+    from jaxdem_gb300 import session
+
+    st = jdem.State.create(pos=np.zeros((4, 2)))
+    sy = jdem.System.create(state=st)
+    stacked = session._stack_frames([(st, sy)])
+    es, ey = session._empty_frames(stacked)
+    assert es.pos_c.shape == (0, 4, 2) and es.q.w.shape == (0, 4, 1)
+    assert np.shape(ey.time) == (0,) and ey.domain.box_size.shape[0] == 0
+
+
 def test_grid_state_lattice():
     st = jdem.utils.grid_state(n_per_axis=(2, 3), spacing=1.5, radius=0.4, seed=1)
     assert st.pos_c.shape == (6, 2)
