@@ -363,6 +363,7 @@ def run_rollout(args, w, young, skin, dev, torch):
             t.append(time.perf_counter() - t0)
         return min(t)
 
+    eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
     eng.rollout(strides[:2], fields=fields, boxes=False)  # graphs for the stride, ring allocation
     plain = best(lambda: eng.step(T * k))
     on_dev = best(lambda: eng.rollout(strides, fields=fields, out=dev_out, boxes=False))

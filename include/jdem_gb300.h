@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 1
+#define JDEM_ABI_VERSION 2
 
 enum {
   JDEM_OK = 0,
@@ -55,6 +55,8 @@ enum {
 enum { JDEM_DOMAIN_FREE = 0, JDEM_DOMAIN_PERIODIC = 1, JDEM_DOMAIN_REFLECT = 2 };
 enum { JDEM_LIN_NONE = 0, JDEM_LIN_VERLET = 1, JDEM_LIN_EULER = 2 };
 enum { JDEM_ROT_NONE = 0, JDEM_ROT_VERLET_SPIRAL = 1, JDEM_ROT_SPIRAL = 2 };
+/* System.force_model: SpringForce (forces/spring.py) or HertzianForce (forces/hertz.py) */
+enum { JDEM_FORCE_SPRING = 0, JDEM_FORCE_HERTZ = 1 };
 
 typedef struct JdemHandle JdemHandle;
 
@@ -79,7 +81,9 @@ typedef struct {
   const JdemSystemDesc* systems;
   float skin;                   /* binning margin; 0 re-sorts every step */
   int32_t n_materials;          /* MaterialTable size M */
-  const float* young_eff;       /* MaterialTable.young_eff, M*M row-major */
+  const float* young_eff;       /* M*M row-major pair constant of the force law: spring k =
+                                   MaterialTable.young_eff; Hertz (4/3) E* with
+                                   1/E* = (1 - nu_i^2)/E_i + (1 - nu_j^2)/E_j (hertz.py:99-105) */
   int32_t bond_width;           /* W of State.bond_id, 0 when there are no bonds */
   int32_t interact_same_bond_id;/* System.interact_same_bond_id */
   int32_t chunk_steps;          /* steps per captured CUDA graph (<= 0: 50) */
@@ -90,6 +94,7 @@ typedef struct {
                                    1: plain graphs (re-sort kernels always launched, returning
                                    early when no re-sort is due; profilers can see every node);
                                    2: no graphs (direct launches) */
+  int32_t force_law;            /* JDEM_FORCE_* */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

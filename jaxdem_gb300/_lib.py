@@ -33,6 +33,7 @@ STATUS_NAMES = {
 DOMAIN = {"free": 0, "periodic": 1, "reflect": 2}
 LINEAR = {"": 0, "verlet": 1, "euler": 2}
 ROTATION = {"": 0, "verletspiral": 1, "spiral": 2}
+FORCE_LAW = {"spring": 0, "hertz": 1}
 
 
 class JdemError(RuntimeError):
@@ -73,6 +74,7 @@ class Config(C.Structure):
         ("device", C.c_int32),
         ("neighbor_list", C.c_int32),
         ("graph_mode", C.c_int32),
+        ("force_law", C.c_int32),
     ]
 
 
@@ -193,7 +195,9 @@ class Engine:
 
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
-                 device: int = 0, neighbor_list=True, graph_mode: int = 0):
+                 device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring"):
+        """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k, or
+        (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``)."""
         self.lib = load()
         self.dim = int(dim)
         self.n_per_system = [int(s["n"]) for s in systems]
@@ -237,6 +241,10 @@ class Engine:
         cfg.neighbor_list = (-1 if neighbor_list is False else
                              (0 if neighbor_list is True else int(neighbor_list)))
         cfg.graph_mode = int(graph_mode)
+        if force_law not in FORCE_LAW:
+            raise ValueError(f"force_law must be one of {sorted(FORCE_LAW)}")
+        cfg.force_law = FORCE_LAW[force_law]
+        self.force_law = force_law
         self._descs = descs
         h = C.c_void_p()
         rc = self.lib.jdem_create(C.byref(cfg), C.byref(h))

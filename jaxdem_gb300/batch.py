@@ -89,12 +89,13 @@ def step_many(states, systems, n: int):
         for k in idx:
             session._check_supported(states[k], systems[k])
         descs = [session._descs(states[k], systems[k])[0] for k in idx]
-        young = np.asarray(systems[idx[0]].mat_table.young_eff, F32)
+        law, young = session.pair_law(systems[idx[0]])
         for k in idx[1:]:
-            if not np.array_equal(np.asarray(systems[k].mat_table.young_eff, F32), young):
-                raise NotImplementedError("systems of one batch must share the material table")
+            lk, yk = session.pair_law(systems[k])
+            if lk != law or not np.array_equal(yk, young):
+                raise NotImplementedError("systems of one batch must share the force law and material table")
         skin = max(session._skin(states[k], systems[k]) for k in idx)
-        eng = Engine(dim, descs, young, skin=skin)
+        eng = Engine(dim, descs, young, skin=skin, force_law=law)
         try:
             cat = lambda f: np.concatenate([np.asarray(f(states[k])) for k in idx])  # noqa: E731
             ad = 3 if dim == 3 else 1

@@ -143,6 +143,8 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   interact_same_bond = cfg->interact_same_bond_id;
   use_nl = cfg->neighbor_list >= 0;
   if (cfg->graph_mode < 0 || cfg->graph_mode > 2) return fail(JDEM_ERR_BAD_ARG, "config: graph_mode in 0..2");
+  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ)
+    return fail(JDEM_ERR_UNSUPPORTED, "config: force_law must be JDEM_FORCE_SPRING or JDEM_FORCE_HERTZ");
   graph_mode = cfg->graph_mode;
   use_conditional = graph_mode == 0;
   nl_request = cfg->neighbor_list;
@@ -160,6 +162,7 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   if ((rc = ensure_capacity(P, S))) return rc;
   b.young = d_young;
   b.n_mat = n_mat;
+  b.law = cfg->force_law == JDEM_FORCE_HERTZ ? LAW_HERTZ : LAW_SPRING;
   b.bond_w = bond_w;
   b.interact_same_bond = interact_same_bond;
   if ((rc = bind_systems())) return rc;

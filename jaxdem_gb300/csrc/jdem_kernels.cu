@@ -519,7 +519,7 @@ __global__ void k_cond(const Ctl* ctl, cudaGraphConditionalHandle h) {
 // The fused step, one thread per slot: particle_step of jdem_pair.cuh, from
 // the slot's Verlet-list row when NL is set and no row overflowed, else from
 // the stencil cells.
-template <int DIM, bool NL, bool GENERAL>
+template <int DIM, bool NL, bool GENERAL, int LAW>
 //
 // 128-thread blocks, at least 10 per SM (48 registers): occupancy hides the
 // dependent list-word -> position gather chain better than the spills cost
@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
   if (t < b.P) {
     const int n = use_list ? b.ncnt[t] : 0;
     const int32_t* nb = use_list ? b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31) : nullptr;
-    d2max = particle_step<DIM, GENERAL>(b, mode, t, sel, ps, use_list, nb, n, 32);
+    d2max = particle_step<DIM, GENERAL, LAW>(b, mode, t, sel, ps, use_list, nb, n, 32);
   }
   if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
 }
@@ -686,8 +686,9 @@ __global__ void k_rot(Bufs b, const int32_t* __restrict__ sys_of, float4* __rest
 
 // ----------------------------------------------------------- diagnostics
 
-// Per-particle energies in caller order: 0.5 * sum_j 0.5 k delta^2
-// (spring.py:110-147, _partition.py:39-51), gravity -m g.x
+// Per-particle energies in caller order: 0.5 * sum_j of the pair energy
+// (spring 0.5 k delta^2, spring.py:110-147; Hertz 0.4 k delta^(5/2),
+// hertz.py:119-160; the 0.5 of _partition.py:39-51), gravity -m g.x
 // (force_manager.py:450-459) and translational kinetic energy
 // (thermal.py:24-47), as doubles; the host sums them in index order.
 template <int DIM>
@@ -739,11 +740,22 @@ __global__ void k_energy(Bufs b, double* __restrict__ out) {
           }
           int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
           float k = b.young[mat_i * b.n_mat + mat_j];
-          float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
-          float rr = dsq * inv;
-          float s = R - rr;
-          s = s > 0.0f ? s : 0.0f;
-          float e = 0.5f * k * (s * s);
+          float e;
+          if (b.law == LAW_HERTZ) {
+            // HertzianForce.energy (hertz.py:149-160): r = norm(r_ij),
+            // E = 0.4 k delta^(5/2), k = (4/3) E* sqrt(R*)
+            float r = dsq == 0.0f ? 0.0f : sqrtf(fmaxf(dsq, 1e-16f));
+            float s = R - r;
+            s = s > 0.0f ? s : 0.0f;
+            float kk = k * sqrtf((pi.w * pj.w) / (pi.w + pj.w));
+            e = 0.4f * kk * ((s * s) * sqrtf(s));
+          } else {
+            float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
+            float rr = dsq * inv;
+            float s = R - rr;
+            s = s > 0.0f ? s : 0.0f;
+            e = 0.5f * k * (s * s);
+          }
           e_pair += (double)(0.5f * e);
         }
       }
@@ -1063,7 +1075,11 @@ void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
   const bool gen = b.n_mat > 1 || (b.bond_w > 0 && !b.interact_same_bond);
   const unsigned int g = nblk(b.P, 128);
-#define JDEM_FORCE(D, L, G) k_force<D, L, G><<<g, 128, 0, st>>>(b, mode)
+#define JDEM_FORCE(D, L, G)                                                    \
+  do {                                                                         \
+    if (b.law == LAW_HERTZ) k_force<D, L, G, LAW_HERTZ><<<g, 128, 0, st>>>(b, mode); \
+    else k_force<D, L, G, LAW_SPRING><<<g, 128, 0, st>>>(b, mode);             \
+  } while (0)
   const bool nl = b.nl_cap > 0;
   if (dim == 3) {
     if (nl) { if (gen) JDEM_FORCE(3, true, true); else JDEM_FORCE(3, true, false); }

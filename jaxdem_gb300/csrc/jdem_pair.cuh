@@ -81,8 +81,9 @@ __device__ __forceinline__ void for_each_candidate(const int32_t* __restrict__ c
   }
 }
 
-// Compensated contact-force accumulator of one particle (spring.py:97-108).
-template <int DIM, bool GENERAL>
+// Compensated contact-force accumulator of one particle: the spring law
+// (spring.py:97-108) or the Hertz law (hertz.py:99-117).
+template <int DIM, bool GENERAL, int LAW>
 struct ContactSum {
   float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
   float4 pi;
@@ -123,20 +124,30 @@ struct ContactSum {
         for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
         if (bonded) return;
       }
-      contact(k, dsq, R, dx, dy, dz);
+      contact(k, dsq, R, pj.w, dx, dy, dz);
     }
   }
 
-  // Spring force of one contact candidate, summed with the two-sum accumulator.
-  __device__ __forceinline__ void contact(float k, float dsq, float R, float dx, float dy, float dz) {
+  // Contact force of one candidate, summed with the two-sum accumulator.
+  __device__ __forceinline__ void contact(float k, float dsq, float R, float rj, float dx, float dy, float dz) {
     float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
     float rr = dsq * inv;
     float delta = R - rr;
     delta = delta > 0.0f ? delta : 0.0f;
-    float mag = k * delta * inv;
-    two_sum_acc(fx, ex, mag * dx);
-    two_sum_acc(fy, ey, mag * dy);
-    if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
+    if (LAW == LAW_HERTZ) {
+      // k = (4/3) E* sqrt(R*), R* = Ri Rj / (Ri + Rj); F = k delta^(3/2) n,
+      // n = r_ij / r (unit_and_norm); delta^(3/2) = delta * sqrt(delta)
+      const float rs = (pi.w * rj) / (pi.w + rj);
+      const float mag = (k * sqrtf(rs)) * (delta * sqrtf(delta));
+      two_sum_acc(fx, ex, mag * (dx * inv));
+      two_sum_acc(fy, ey, mag * (dy * inv));
+      if (DIM == 3) two_sum_acc(fz, ez, mag * (dz * inv));
+    } else {
+      float mag = k * delta * inv;
+      two_sum_acc(fx, ex, mag * dx);
+      two_sum_acc(fy, ey, mag * dy);
+      if (DIM == 3) two_sum_acc(fz, ez, mag * dz);
+    }
   }
 };
 
@@ -213,7 +224,7 @@ __device__ __forceinline__ float integrate_particle(const Bufs& b, int mode, lon
 // `nb` (n slot indices, `stride` ints apart) when use_list is set, else from
 // the stencil cells (periodic minimum image of periodic.py:74-79), then
 // integrate_particle.
-template <int DIM, bool GENERAL>
+template <int DIM, bool GENERAL, int LAW>
 __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long long t, unsigned int sel,
                                                unsigned int ps, bool use_list, const int32_t* __restrict__ nb,
                                                int n, int stride) {
@@ -221,7 +232,7 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
   const float4 pi = P[t];
   const uint32_t tg = b.tag[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
-  ContactSum<DIM, GENERAL> acc(b, sp, pi, tg, sel, t);
+  ContactSum<DIM, GENERAL, LAW> acc(b, sp, pi, tg, sel, t);
   if (use_list) {
     for (int k = 0; k < n; k += 4) {
       uint32_t e[4];

@@ -1,8 +1,8 @@
 """Force model and force manager (``jaxdem/forces``).
 
-``SpringForce`` (``forces/spring.py:69-147``) is evaluated on the device by
-the collider kernels; this class carries its identity and material
-requirements.  ``ForceManager`` (``forces/force_manager.py``) carries gravity
+``SpringForce`` (``forces/spring.py:69-147``) and ``HertzianForce``
+(``forces/hertz.py:22-170``) are evaluated on the device by the collider
+kernels; these classes carry their identity and material requirements.  ``ForceManager`` (``forces/force_manager.py``) carries gravity
 and the per-step external buffers; the device applies gravity
 (``force_manager.py:393-397``) inside the fused step kernel.
 """
@@ -37,6 +37,30 @@ class SpringForce(ForceModel):
     @property
     def required_material_properties(self) -> tuple:
         return ("young_eff",)
+
+
+@ForceModel.register("hertz")
+@dataclass
+class HertzianForce(ForceModel):
+    """Hertz normal contact (``forces/hertz.py:22-170``): F = k delta^(3/2) n,
+    E = 0.4 k delta^(5/2), k = (4/3) E* sqrt(R*), R* = Ri Rj / (Ri + Rj), with E*
+    from the per-material ``young`` and ``poisson`` (no matchmaker)."""
+
+    @property
+    def required_material_properties(self) -> tuple:
+        return ("young", "poisson")
+
+
+def hertz_pair_constant(young, poisson) -> np.ndarray:
+    """(M, M) float32 table of (4/3) E*, in the reference's float32 order
+    (``hertz.py:99-105``): E* = 1 / ((1 - nu_i**2) / E_i + (1 - nu_j**2) / E_j),
+    then (4/3) * E*.  The device multiplies it by sqrt(R*) per pair."""
+    E = np.asarray(young, F32).reshape(-1)
+    nu = np.asarray(poisson, F32).reshape(-1)
+    a = (F32(1.0) - nu * nu) / E
+    with np.errstate(divide="ignore"):
+        e_star = (F32(1.0) / (a[:, None] + a[None, :])).astype(F32)
+    return (F32(4.0 / 3.0) * e_star).astype(F32)
 
 
 @dataclass

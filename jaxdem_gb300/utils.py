@@ -1,8 +1,9 @@
 """Energy and contact utilities (``jaxdem/utils/thermal.py``, ``jaxdem/utils/contacts.py``).
 
 Energies and neighbour lists are evaluated by the GB300 engine; the per-pair
-spring force of ``get_pair_forces_and_ids`` is restated on the host from the
-device neighbour list with the same float32 operations as ``spring.py:97-108``.
+force of ``get_pair_forces_and_ids`` is restated on the host from the device
+neighbour list with the same float32 operations as ``spring.py:97-108`` or
+``hertz.py:99-117``.
 """
 
 from __future__ import annotations
@@ -63,13 +64,22 @@ def get_pair_forces_and_ids(state, system, cutoff=None, max_neighbors=None):
     d_sq = rij[:, 0] * rij[:, 0]
     for a in range(1, d):
         d_sq = d_sq + rij[:, a] * rij[:, a]
-    R = state.rad[i_ids] + state.rad[sj]
-    k = np.asarray(system.mat_table.young_eff, F32)[state.mat_id[i_ids], state.mat_id[sj]]
-    with np.errstate(divide="ignore"):
+    ri, rj = state.rad[i_ids], state.rad[sj]
+    R = ri + rj
+    law, table = session.pair_law(system)
+    k = table[state.mat_id[i_ids], state.mat_id[sj]]
+    with np.errstate(divide="ignore", invalid="ignore"):
         inv = np.where(d_sq == 0, F32(0), F32(1) / np.sqrt(np.maximum(d_sq, F32(1e-16))))
     r = d_sq * inv
     delta = np.maximum(F32(0), R - r) * (i_ids != sj).astype(F32)
-    f = ((k * delta * inv)[:, None] * rij).astype(F32) * valid[:, None]
+    if law == "hertz":
+        # hertz.py:99-117: k = (4/3) E* sqrt(R*), F = k delta^(3/2) (r_ij / r)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            kk = k * np.sqrt((ri * rj) / R)
+        mag = np.where(valid, kk * np.power(delta, F32(1.5)), F32(0))
+        f = (mag[:, None] * (rij * inv[:, None])).astype(F32) * valid[:, None]
+    else:
+        f = ((k * delta * inv)[:, None] * rij).astype(F32) * valid[:, None]
     return state, system, np.column_stack((i_ids, j_ids)), f.astype(F32)
 
 

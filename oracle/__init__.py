@@ -24,6 +24,7 @@ CFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-s
 
 DOMAIN = {"free": 0, "periodic": 1, "reflect": 2}
 LINEAR = {"": 0, "verlet": 1, "euler": 2}
+LAW = {"spring": 0, "hertz": 1}
 
 def build_c(force: bool = False) -> Path:
     """Compile the C restatement twice (float32 and float64; gcc, OpenMP, no FMA contraction)."""
@@ -52,11 +53,11 @@ def load_c(f64: bool = False) -> C.CDLL:
         real = C.c_double if f64 else C.c_float
         step = getattr(lib, "oracle_step" + sfx)
         step.argtypes = [C.c_int, C.c_int64, C.c_int, fp, fp, real, fp, real, real, C.c_int, C.c_int, fp, C.c_int,
-                         fp, fp, fp, fp, fp, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, fp, fp]
+                         fp, fp, fp, fp, fp, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, fp, fp, C.c_int]
         step.restype = C.c_int
         force = getattr(lib, "oracle_force" + sfx)
         force.argtypes = [C.c_int, C.c_int64, C.c_int, fp, fp, real, C.c_int, C.c_int, fp, fp, fp, C.c_void_p, fp,
-                          C.c_int, C.c_int]
+                          C.c_int, C.c_int, C.c_int]
         force.restype = C.c_int
         getattr(lib, "oracle_max_threads" + sfx).restype = C.c_int
         lib.step, lib.force, lib.max_threads = step, force, getattr(lib, "oracle_max_threads" + sfx)
@@ -70,9 +71,10 @@ def _p(a):
 
 def c_step(dim, pos, vel, force, rad, mass, *, domain, box, anchor, dt, steps, cell_size, search_range=1,
            young=None, gravity=None, restitution=1.0, linear="verlet", mat_id=None, fixed=None, threads=0,
-           acc64=False):
+           acc64=False, law="spring"):
     """Run ``steps`` reference steps in place; float32 arrays use the float
-    build, float64 arrays the double build.  Returns (box, anchor)."""
+    build, float64 arrays the double build.  ``young`` is the force law's pair
+    constant (spring k, or (4/3) E* for ``law="hertz"``).  Returns (box, anchor)."""
     f64 = pos.dtype == np.float64
     T = np.float64 if f64 else np.float32
     lib = load_c(f64)
@@ -93,14 +95,14 @@ def c_step(dim, pos, vel, force, rad, mass, *, domain, box, anchor, dt, steps, c
     rc = lib.step(dim, N, DOMAIN[domain], _p(box3), _p(anc3), float(restitution), _p(g3), float(dt),
                   float(cell_size), int(search_range), young.shape[0], _p(young), LINEAR[linear],
                   _p(pos), _p(vel), _p(force), _p(rad), _p(mass), mat.ctypes.data, fx.ctypes.data,
-                  int(steps), int(threads), int(acc64), _p(bo), _p(ao))
+                  int(steps), int(threads), int(acc64), _p(bo), _p(ao), LAW[law])
     if rc != 0:
         raise RuntimeError(f"oracle_step failed ({rc})")
     return bo[:dim].copy(), ao[:dim].copy()
 
 
 def c_force(dim, pos, rad, *, domain, box, anchor, cell_size, search_range=1, young=None, mat_id=None,
-            threads=0, acc64=False):
+            threads=0, acc64=False, law="spring"):
     f64 = np.asarray(pos).dtype == np.float64
     T = np.float64 if f64 else np.float32
     lib = load_c(f64)
@@ -114,7 +116,8 @@ def c_force(dim, pos, rad, *, domain, box, anchor, cell_size, search_range=1, yo
     mat = np.zeros(N, np.int32) if mat_id is None else np.ascontiguousarray(mat_id, np.int32)
     out = np.zeros((N, dim), T)
     rc = lib.force(dim, N, DOMAIN[domain], _p(box3), _p(anc3), float(cell_size), int(search_range),
-                   young.shape[0], _p(young), _p(pos), _p(rad), mat.ctypes.data, _p(out), int(threads), int(acc64))
+                   young.shape[0], _p(young), _p(pos), _p(rad), mat.ctypes.data, _p(out), int(threads), int(acc64),
+                   LAW[law])
     if rc != 0:
         raise RuntimeError(f"oracle_force failed ({rc})")
     return out

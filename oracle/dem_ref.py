@@ -82,7 +82,7 @@ class OSystem:
     domain: str  # "periodic" | "reflect" | "free"
     box_size: np.ndarray
     anchor: np.ndarray
-    young_eff: np.ndarray  # (M, M)
+    young_eff: np.ndarray  # (M, M): spring k, or (4/3) E* when force_law == "hertz"
     dt: np.floating
     cell_size: np.floating
     neighbor_mask: np.ndarray  # (M_st, d) int
@@ -94,6 +94,7 @@ class OSystem:
     time: np.floating = np.float32(0.0)
     step_count: int = 0
     inv_box_size: Optional[np.ndarray] = None
+    force_law: str = "spring"  # "spring" (forces/spring.py) | "hertz" (forces/hertz.py)
 
     def __post_init__(self) -> None:
         if self.inv_box_size is None:
@@ -326,6 +327,64 @@ def spring_energy_pair(i, j, pos, rad, mat_id, young_eff, sy: OSystem):
     return dt(0.5) * k * s * s
 
 
+def hertz_constant(young, poisson):
+    """(M, M) table (4/3) E* of ``HertzianForce`` (``forces/hertz.py:99-105``), float32:
+    E* = 1 / ((1 - nu_i**2) / E_i + (1 - nu_j**2) / E_j)."""
+    E = np.asarray(young, np.float32).reshape(-1)
+    nu = np.asarray(poisson, np.float32).reshape(-1)
+    a = (np.float32(1.0) - nu ** 2) / E
+    return (np.float32(4.0 / 3.0) * (np.float32(1.0) / (a[:, None] + a[None, :]))).astype(np.float32)
+
+
+def hertz_pair(i, j, pos, rad, mat_id, k43, sy: OSystem):
+    """``HertzianForce.force`` (``forces/hertz.py:63-117``), vectorised over pairs:
+    k = (4/3) E* sqrt(R*), R* = Ri Rj / (Ri + Rj); F = k pow(delta, 1.5) n with
+    (n, r) = unit_and_norm(r_ij) (``utils/linalg.py:164-181``)."""
+    dt = pos.dtype.type
+    Ri, Rj = rad[i], rad[j]
+    R_star = (Ri * Rj) / (Ri + Rj)
+    k = k43[mat_id[i], mat_id[j]] * np.sqrt(R_star)
+    rij = displacement_fast(pos[i], pos[j], sy)
+    n2 = sumsq(rij)
+    safe = np.maximum(n2, dt(1e-16))
+    with np.errstate(divide="ignore"):
+        inv = np.where(n2 == 0, dt(0), dt(1) / np.sqrt(safe))
+    r = n2 * inv
+    n = rij * inv[..., None]
+    delta = np.maximum(dt(0), Ri + Rj - r) * (np.asarray(i) != np.asarray(j)).astype(pos.dtype)
+    mag = k * np.power(delta, dt(1.5))
+    return mag[..., None] * n
+
+
+def hertz_energy_pair(i, j, pos, rad, mat_id, k43, sy: OSystem):
+    """``HertzianForce.energy`` (``forces/hertz.py:119-160``): 0.4 k pow(delta, 2.5)
+    with r = norm(r_ij) (``utils/linalg.py:115-133``)."""
+    dt = pos.dtype.type
+    Ri, Rj = rad[i], rad[j]
+    R_star = (Ri * Rj) / (Ri + Rj)
+    k = k43[mat_id[i], mat_id[j]] * np.sqrt(R_star)
+    rij = displacement_fast(pos[i], pos[j], sy)
+    n2 = sumsq(rij)
+    r = np.where(n2 == 0, dt(0), np.sqrt(np.maximum(n2, dt(1e-16))))
+    delta = Ri + Rj - r
+    delta = delta * (delta > 0).astype(pos.dtype) * (np.asarray(i) != np.asarray(j)).astype(pos.dtype)
+    return dt(0.4) * k * np.power(delta, dt(2.5))
+
+
+def pair_force(i, j, pos, rad, mat_id, sy: OSystem):
+    """The force law of ``sy`` (``System.force_model.force``)."""
+    if sy.force_law == "hertz":
+        return hertz_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
+    return spring_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
+
+
+def pair_energy(i, j, pos, rad, mat_id, sy: OSystem):
+    """The force law's pair energy (``System.force_model.energy``)."""
+    if sy.force_law == "hertz":
+        return hertz_energy_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
+    return spring_energy_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
+
+
 def valid_mask(clump_i, clump_j, bond_row_i, index_j, interact_same_bond_id):
     """``valid_interaction_mask`` (``colliders/__init__.py:225-243``)."""
     is_bonded = np.any(bond_row_i == np.asarray(index_j)[..., None], axis=-1)
@@ -383,7 +442,7 @@ def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     d = st.dim
 
     def pair(i, j):
-        return spring_pair(i, j, pos, st.rad, st.mat_id, sy.young_eff, sy)
+        return pair_force(i, j, pos, st.rad, st.mat_id, sy)
 
     f = _traverse(st, sy, pair, (d,), pos.dtype, sum_dtype)
     return f.astype(pos.dtype), np.zeros_like(st.torque)
@@ -395,7 +454,7 @@ def cell_list_energy(st: OState, sy: OSystem, sum_dtype=None):
     half = pos.dtype.type(0.5)
 
     def pair(i, j):
-        return half * spring_energy_pair(i, j, pos, st.rad, st.mat_id, sy.young_eff, sy)
+        return half * pair_energy(i, j, pos, st.rad, st.mat_id, sy)
 
     e = _traverse(st, sy, pair, (), pos.dtype, sum_dtype)
     return e.sum(dtype=np.float64)
@@ -408,7 +467,7 @@ def naive_force(st: OState, sy: OSystem, sum_dtype=np.float64):
     iota = np.arange(N)
     out = np.zeros((N, st.dim), sum_dtype)
     for i in range(N):
-        f = spring_pair(np.full(N, i), iota, pos, st.rad, st.mat_id, sy.young_eff, sy)
+        f = pair_force(np.full(N, i), iota, pos, st.rad, st.mat_id, sy)
         ok = valid_mask(st.clump_id[i], st.clump_id, st.bond_id[i][None, :], iota,
                         sy.interact_same_bond_id)
         out[i] = np.where(ok[:, None], f, 0).astype(sum_dtype).sum(axis=0)
@@ -725,7 +784,7 @@ def naive_energy(st: OState, sy: OSystem) -> float:
     N = st.N
     ii, jj = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
     ii, jj = ii.ravel(), jj.ravel()
-    e = spring_energy_pair(ii, jj, st.pos_c, st.rad, st.mat_id, sy.young_eff, sy)
+    e = pair_energy(ii, jj, st.pos_c, st.rad, st.mat_id, sy)
     ok = valid_mask(st.clump_id[ii], st.clump_id[jj], st.bond_id[ii], jj, sy.interact_same_bond_id)
     return float(np.sum(np.where(ok, st.pos_c.dtype.type(0.5) * e, 0).astype(np.float64)))
 

@@ -13,6 +13,7 @@
  *   partition + stencil    jaxdem/colliders/cell_list.py:35-96
  *   pair traversal         jaxdem/colliders/cell_list.py:187-261 (chunks of 4)
  *   spring force           jaxdem/forces/spring.py:69-108
+ *   Hertz force            jaxdem/forces/hertz.py:63-117 (young_eff holds (4/3) E*)
  *   periodic displacement  jaxdem/domains/periodic.py:74-79 (rint = half-even)
  *   reflect walls + TOC    jaxdem/domains/reflect.py:99-299, _toc.py:11-94
  *   free bounding box      jaxdem/domains/free.py:40-63
@@ -55,6 +56,7 @@ typedef double real;
 #define R_RINT rint_d
 #define R_FMOD fmod
 #define R_FABS fabs
+#define R_POW pow
 #else
 typedef float real;
 #define FN(name) name
@@ -64,6 +66,7 @@ typedef float real;
 #define R_RINT rint_f
 #define R_FMOD fmodf
 #define R_FABS fabsf
+#define R_POW powf
 #endif
 #include <stdlib.h>
 #include <string.h>
@@ -83,7 +86,8 @@ typedef struct {
   real cell[3];
   int64_t ncell;
   int n_mat;
-  const real* young;
+  const real* young; /* spring k, or (4/3) E* for the Hertz law */
+  int law;           /* 0 spring, 1 Hertz */
 } Grid;
 
 static void grid_setup(Grid* G) {
@@ -171,6 +175,30 @@ static inline void spring_pair(const Grid* G, const real* pi, const real* pj, re
   for (int a = 0; a < d; ++a) f[a] = mag * rij[a];
 }
 
+/* Force on i due to j: hertz.py:99-117.  k43 = (4/3) E*; k = k43 sqrt(R*),
+ * (n, r) = unit_and_norm(r_ij) (utils/linalg.py:164-181), F = k pow(delta, 1.5) n. */
+static inline void hertz_pair(const Grid* G, const real* pi, const real* pj, real ri, real rj,
+                              real k43, int same, real* f) {
+  int d = G->dim;
+  real rij[3];
+  real R_star = (ri * rj) / (ri + rj);
+  real k = k43 * R_SQRT(R_star);
+  for (int a = 0; a < d; ++a) {
+    real x = pi[a] - pj[a];
+    if (G->domain == DOM_PERIODIC) x = x - G->box[a] * R_RINT(x * G->inv_box[a]);
+    rij[a] = x;
+  }
+  real n2 = rij[0] * rij[0];
+  for (int a = 1; a < d; ++a) n2 = n2 + rij[a] * rij[a];
+  real inv = (n2 == 0.0f) ? 0.0f : 1.0f / R_SQRT(n2 > 1e-16f ? n2 : 1e-16f);
+  real r = n2 * inv;
+  real delta = (ri + rj) - r;
+  if (!(delta > 0.0f)) delta = 0.0f;
+  delta = delta * (same ? 0.0f : 1.0f);
+  real mag = k * R_POW(delta, (real)1.5);
+  for (int a = 0; a < d; ++a) f[a] = mag * (rij[a] * inv);
+}
+
 /* compute_force via the cell list in the reference's visiting order. */
 static void cell_list_force(const Grid* G, int64_t n, const real* pos, const real* rad,
                             const int32_t* mat, const int64_t* hash, const int64_t* start,
@@ -232,7 +260,10 @@ static void cell_list_force(const Grid* G, int64_t n, const real* pos, const rea
           int64_t j = perm[k + u];
           real f[3];
           real kk = G->young[mat[i] * G->n_mat + mat[j]];
-          spring_pair(G, pos + i * d, pos + j * d, rad[i], rad[j], kk, i == j, f);
+          if (G->law == 1)
+            hertz_pair(G, pos + i * d, pos + j * d, rad[i], rad[j], kk, i == j, f);
+          else
+            spring_pair(G, pos + i * d, pos + j * d, rad[i], rad[j], kk, i == j, f);
           for (int a = 0; a < d; ++a) {
             chunk[a] = chunk[a] + f[a];
             acc64v[a] += (double)f[a];
@@ -323,7 +354,7 @@ int FN(oracle_step)(int dim, int64_t n, int domain, const real* box_in, const re
                 int search_range, int n_mat, const real* young_eff, int linear, real* pos,
                 real* vel, real* force, const real* rad, const real* mass,
                 const int32_t* mat_id, const uint8_t* fixed, int64_t steps, int n_threads,
-                int acc64, real* box_out, real* anchor_out) {
+                int acc64, real* box_out, real* anchor_out, int law) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #endif
@@ -336,6 +367,7 @@ int FN(oracle_step)(int dim, int64_t n, int domain, const real* box_in, const re
   G.sr = search_range;
   G.n_mat = n_mat;
   G.young = young_eff;
+  G.law = law;
   for (int a = 0; a < dim; ++a) {
     G.box[a] = box_in[a];
     G.anchor[a] = anchor_in[a];
@@ -419,7 +451,7 @@ int FN(oracle_step)(int dim, int64_t n, int domain, const real* box_in, const re
 int FN(oracle_force)(int dim, int64_t n, int domain, const real* box, const real* anchor,
                  real cell_size, int search_range, int n_mat, const real* young_eff,
                  const real* pos, const real* rad, const int32_t* mat_id, real* force,
-                 int n_threads, int acc64) {
+                 int n_threads, int acc64, int law) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #endif
@@ -431,6 +463,7 @@ int FN(oracle_force)(int dim, int64_t n, int domain, const real* box, const real
   G.sr = search_range;
   G.n_mat = n_mat;
   G.young = young_eff;
+  G.law = law;
   for (int a = 0; a < dim; ++a) {
     G.box[a] = box[a];
     G.anchor[a] = anchor[a];

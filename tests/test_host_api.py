@@ -117,6 +117,27 @@ def test_trajectory_rollout_argument_checks():
         jdem.System.trajectory_rollout(st, sy, strides=np.ones((2, 2), int))
 
 
+def test_hertz_force_model_pair_constant():
+    """HertzianForce (forces/hertz.py:22-170) reads young and poisson per material; the
+    engine receives (4/3) E* per material pair in the reference's float32 order."""
+    from jaxdem_gb300 import session
+    from oracle import dem_ref as R
+
+    mats = [jdem.Material.create("elastic", young=1e3, poisson=0.3),
+            jdem.Material.create("elastic", young=4e3, poisson=0.2)]
+    table = jdem.MaterialTable.from_materials(mats)
+    st = jdem.State.create(pos=np.zeros((2, 3)), mat_table=table)
+    sy = jdem.System.create(state=st, mat_table=table, force_model_type="hertz")
+    assert type(sy.force_model).__name__ == "HertzianForce"
+    law, k = session.pair_law(sy)
+    assert law == "hertz" and k.dtype == F32
+    assert np.array_equal(k, R.hertz_constant([1e3, 4e3], [0.3, 0.2]))
+    e_star = 1.0 / ((1 - 0.09) / 1e3 + (1 - 0.04) / 4e3)
+    assert np.isclose(k[0, 1], 4.0 / 3.0 * e_star, rtol=1e-6) and k[0, 1] == k[1, 0]
+    law, k = session.pair_law(jdem.System.create(state=st, mat_table=table))
+    assert law == "spring" and np.array_equal(k, table.young_eff)
+
+
 def test_rollout_frame_times_match_stepwise_float32():
     """Frame times of a rollout: float32 ``time += dt`` once per step (system.py:62-66),
     for a scalar system and for a batch with per-member dt and time."""

@@ -10,7 +10,9 @@ analytic cases, on the numpy and C restatements:
   Euler > 0.7, spheres in periodic / reflect / free domains, 2D and 3D;
 * ``tests/test_rotation_integrators.py:24-97``: torque-driven asymmetric body
   against the closed form, relative error < 1e-4;
-* two overlapping spheres (|F| = k delta), a periodic image pair, a wall bounce.
+* two overlapping spheres (|F| = k delta), a periodic image pair, a wall bounce;
+* the Hertz law (no reference test covers it): two spheres against the closed
+  form, F = -dE/dd, and the C restatement against numpy.
 """
 
 from __future__ import annotations
@@ -62,6 +64,70 @@ def test_two_sphere_spring_analytic():
     assert np.allclose(f[0], [-k * delta, 0, 0], rtol=1e-6)
     assert np.allclose(f[1], [k * delta, 0, 0], rtol=1e-6)
     assert np.isclose(R.cell_list_energy(st, sy), 0.5 * k * delta ** 2, rtol=1e-6)
+
+
+def test_two_sphere_hertz_analytic():
+    """Hertz law (forces/hertz.py:22-170), hand-derived: 1/E* = 2 (1 - nu^2) / E for two
+    spheres of one material, R* = r0 r1 / (r0 + r1), k = (4/3) E* sqrt(R*),
+    |F| = k delta^(3/2) along r_hat, E = (2/5) k delta^(5/2); and F = -dE/dd by a
+    central difference of the float64 oracle."""
+    E, nu, r0, r1 = 1e3, 0.3, 0.5, 0.7
+    k43 = R.hertz_constant([E], [nu])
+    assert np.isclose(k43[0, 0], 4.0 / 3.0 * E / (2 * (1 - nu * nu)), rtol=1e-6)
+    k = 4.0 / 3.0 * E / (2 * (1 - nu * nu)) * np.sqrt(r0 * r1 / (r0 + r1))
+    rad = np.array([r0, r1], F32)
+
+    def hertz_sys(dtype):
+        s = _sys(3, domain="free", rad=rad, dtype=dtype)
+        s.young_eff = k43.astype(dtype)
+        s.force_law = "hertz"
+        return s
+
+    for d in (1.0, 1.1, 1.19):
+        pos = np.array([[1.0, 2.0, 3.0], [1.0 + d, 2.0, 3.0]], F32)
+        st = R.make_state(pos, rad=rad)
+        f, _ = R.cell_list_force(st, hertz_sys(F32), sum_dtype=np.float64)
+        # the overlap of the stored float32 radii and coordinates; float32 R - r loses
+        # about one ulp of r (1.2e-7 r) to cancellation, amplified 3/2 by delta^(3/2)
+        delta = float(rad[0]) + float(rad[1]) - (float(pos[1, 0]) - float(pos[0, 0]))
+        tol = 2e-6 + 3.0 * 1.2e-7 * d / delta
+        assert np.allclose(f[0], [-k * delta ** 1.5, 0, 0], rtol=tol)
+        assert np.allclose(f[1], [k * delta ** 1.5, 0, 0], rtol=tol)
+        assert np.isclose(R.cell_list_energy(st, hertz_sys(F32)), 0.4 * k * delta ** 2.5, rtol=2 * tol)
+        assert np.allclose(R.naive_force(st, hertz_sys(F32)), f, rtol=1e-6)
+    # the force is minus the energy gradient (float64 oracle)
+    sy64 = hertz_sys(np.float64)
+    d, h = 1.05, 1e-6
+
+    def energy(dd):
+        p = np.array([[1.0, 2.0, 3.0], [1.0 + dd, 2.0, 3.0]])
+        return R.cell_list_energy(R.make_state(p, rad=rad, dtype=np.float64), sy64)
+
+    p = np.array([[1.0, 2.0, 3.0], [1.0 + d, 2.0, 3.0]])
+    f64, _ = R.cell_list_force(R.make_state(p, rad=rad, dtype=np.float64), sy64)
+    assert np.isclose(f64[1, 0], -(energy(d + h) - energy(d - h)) / (2 * h), rtol=1e-6)
+    # apart: no force
+    st = R.make_state(np.array([[0.0, 0, 0], [1.3, 0, 0]], F32), rad=rad)
+    assert not np.any(R.cell_list_force(st, hertz_sys(F32))[0])
+
+
+def test_hertz_c_restatement_matches_numpy():
+    """The C/OpenMP Hertz law against the numpy oracle on a polydisperse, two-material
+    periodic packing: agreement to the last bits of pow (different libm routines)."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    N, L = 2000, 13.0
+    pos = rng.uniform(0, L, (N, 3)).astype(F32)
+    rad = rng.choice([0.5, 0.6, 0.7], N).astype(F32)
+    mat = rng.integers(0, 2, N).astype(np.int32)
+    k43 = R.hertz_constant([1e3, 4e3], [0.3, 0.2])
+    st = R.make_state(pos, rad=rad, mat_id=mat)
+    sy = _sys(3, domain="periodic", box=[L] * 3, rad=rad)
+    sy.young_eff, sy.force_law = k43, "hertz"
+    f, _ = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    fc = oracle.c_force(3, pos, rad, domain="periodic", box=sy.box_size, anchor=sy.anchor,
+                        cell_size=float(sy.cell_size), young=k43, mat_id=mat, acc64=True, law="hertz")
+    scale = np.abs(f).max()
+    assert scale > 0 and np.abs(f - fc).max() <= 1e-6 * scale
 
 
 def test_periodic_image_pair():
