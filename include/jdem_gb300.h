@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 2
+#define JDEM_ABI_VERSION 3
 
 enum {
   JDEM_OK = 0,
@@ -55,8 +55,9 @@ enum {
 enum { JDEM_DOMAIN_FREE = 0, JDEM_DOMAIN_PERIODIC = 1, JDEM_DOMAIN_REFLECT = 2 };
 enum { JDEM_LIN_NONE = 0, JDEM_LIN_VERLET = 1, JDEM_LIN_EULER = 2 };
 enum { JDEM_ROT_NONE = 0, JDEM_ROT_VERLET_SPIRAL = 1, JDEM_ROT_SPIRAL = 2 };
-/* System.force_model: SpringForce (forces/spring.py) or HertzianForce (forces/hertz.py) */
-enum { JDEM_FORCE_SPRING = 0, JDEM_FORCE_HERTZ = 1 };
+/* System.force_model: SpringForce (forces/spring.py), HertzianForce (forces/hertz.py) or
+ * CundallStrackForce (forces/cundall_strack.py) */
+enum { JDEM_FORCE_SPRING = 0, JDEM_FORCE_HERTZ = 1, JDEM_FORCE_CUNDALL_STRACK = 2 };
 
 typedef struct JdemHandle JdemHandle;
 
@@ -83,7 +84,9 @@ typedef struct {
   int32_t n_materials;          /* MaterialTable size M */
   const float* young_eff;       /* M*M row-major pair constant of the force law: spring k =
                                    MaterialTable.young_eff; Hertz (4/3) E* with
-                                   1/E* = (1 - nu_i^2)/E_i + (1 - nu_j^2)/E_j (hertz.py:99-105) */
+                                   1/E* = (1 - nu_i^2)/E_i + (1 - nu_j^2)/E_j (hertz.py:99-105);
+                                   Cundall-Strack the damping ratio beta of e = min(e_i, e_j)
+                                   (cundall_strack.py:143-150) */
   int32_t bond_width;           /* W of State.bond_id, 0 when there are no bonds */
   int32_t interact_same_bond_id;/* System.interact_same_bond_id */
   int32_t chunk_steps;          /* steps per captured CUDA graph (<= 0: 50) */
@@ -95,6 +98,8 @@ typedef struct {
                                    early when no re-sort is due; profilers can see every node);
                                    2: no graphs (direct launches) */
   int32_t force_law;            /* JDEM_FORCE_* */
+  const float* material_props;  /* Cundall-Strack only: M*4 per material (young, shear modulus
+                                   young / (2 (1 + poisson)), mu, mu_r) */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

@@ -33,7 +33,7 @@ STATUS_NAMES = {
 DOMAIN = {"free": 0, "periodic": 1, "reflect": 2}
 LINEAR = {"": 0, "verlet": 1, "euler": 2}
 ROTATION = {"": 0, "verletspiral": 1, "spiral": 2}
-FORCE_LAW = {"spring": 0, "hertz": 1}
+FORCE_LAW = {"spring": 0, "hertz": 1, "cundallstrack": 2}
 
 
 class JdemError(RuntimeError):
@@ -75,6 +75,7 @@ class Config(C.Structure):
         ("neighbor_list", C.c_int32),
         ("graph_mode", C.c_int32),
         ("force_law", C.c_int32),
+        ("material_props", C.POINTER(C.c_float)),
     ]
 
 
@@ -195,9 +196,12 @@ class Engine:
 
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
-                 device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring"):
-        """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k, or
-        (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``)."""
+                 device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring",
+                 material_props: Optional[np.ndarray] = None):
+        """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k,
+        (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``), or the damping ratio
+        beta for ``"cundallstrack"``, which also takes ``material_props`` (M, 4)
+        (``forces.cundall_strack_tables``)."""
         self.lib = load()
         self.dim = int(dim)
         self.n_per_system = [int(s["n"]) for s in systems]
@@ -245,6 +249,12 @@ class Engine:
             raise ValueError(f"force_law must be one of {sorted(FORCE_LAW)}")
         cfg.force_law = FORCE_LAW[force_law]
         self.force_law = force_law
+        self._props = None
+        if material_props is not None:
+            self._props = np.ascontiguousarray(material_props, np.float32).reshape(-1, 4)
+            if self._props.shape[0] != self._young.shape[0]:
+                raise ValueError("material_props must have one row of 4 per material")
+            cfg.material_props = self._props.ctypes.data_as(C.POINTER(C.c_float))
         self._descs = descs
         h = C.c_void_p()
         rc = self.lib.jdem_create(C.byref(cfg), C.byref(h))

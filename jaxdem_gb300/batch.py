@@ -89,13 +89,13 @@ def step_many(states, systems, n: int):
         for k in idx:
             session._check_supported(states[k], systems[k])
         descs = [session._descs(states[k], systems[k])[0] for k in idx]
-        law, young = session.pair_law(systems[idx[0]])
+        law, young, props = session.pair_law(systems[idx[0]])
         for k in idx[1:]:
-            lk, yk = session.pair_law(systems[k])
-            if lk != law or not np.array_equal(yk, young):
+            lk, yk, pk = session.pair_law(systems[k])
+            if lk != law or not np.array_equal(yk, young) or (props is not None and not np.array_equal(pk, props)):
                 raise NotImplementedError("systems of one batch must share the force law and material table")
         skin = max(session._skin(states[k], systems[k]) for k in idx)
-        eng = Engine(dim, descs, young, skin=skin, force_law=law)
+        eng = Engine(dim, descs, young, skin=skin, force_law=law, material_props=props)
         try:
             cat = lambda f: np.concatenate([np.asarray(f(states[k])) for k in idx])  # noqa: E731
             ad = 3 if dim == 3 else 1

@@ -143,8 +143,11 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   interact_same_bond = cfg->interact_same_bond_id;
   use_nl = cfg->neighbor_list >= 0;
   if (cfg->graph_mode < 0 || cfg->graph_mode > 2) return fail(JDEM_ERR_BAD_ARG, "config: graph_mode in 0..2");
-  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ)
-    return fail(JDEM_ERR_UNSUPPORTED, "config: force_law must be JDEM_FORCE_SPRING or JDEM_FORCE_HERTZ");
+  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ &&
+      cfg->force_law != JDEM_FORCE_CUNDALL_STRACK)
+    return fail(JDEM_ERR_UNSUPPORTED, "config: unknown force_law");
+  if (cfg->force_law == JDEM_FORCE_CUNDALL_STRACK && !cfg->material_props)
+    return fail(JDEM_ERR_BAD_ARG, "config: Cundall-Strack needs material_props");
   graph_mode = cfg->graph_mode;
   use_conditional = graph_mode == 0;
   nl_request = cfg->neighbor_list;
@@ -162,7 +165,15 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   if ((rc = ensure_capacity(P, S))) return rc;
   b.young = d_young;
   b.n_mat = n_mat;
-  b.law = cfg->force_law == JDEM_FORCE_HERTZ ? LAW_HERTZ : LAW_SPRING;
+  b.law = cfg->force_law == JDEM_FORCE_HERTZ ? LAW_HERTZ
+          : cfg->force_law == JDEM_FORCE_CUNDALL_STRACK ? LAW_CS : LAW_SPRING;
+  if (b.law == LAW_CS) {
+    float* d_mprop = nullptr;
+    if ((rc = dalloc((void**)&d_mprop, sizeof(float) * 4 * n_mat))) return rc;
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_mprop, cfg->material_props, sizeof(float) * 4 * n_mat,
+                                        cudaMemcpyHostToDevice, stream));
+    b.mprop = d_mprop;
+  }
   b.bond_w = bond_w;
   b.interact_same_bond = interact_same_bond;
   if ((rc = bind_systems())) return rc;
@@ -252,6 +263,12 @@ int JdemHandle::ensure_capacity(long long p_need, int s_need) {
     s_cap = cap;
   }
   b.bond = d_bond;
+  b.rq = (float4*)d_q;
+  b.rw = d_w;
+  b.rtq = d_tq;
+  b.rinertia = d_inertia;
+  b.sys_of = st_sys;
+  b.fixed_c = st_fixed;
   return JDEM_OK;
 }
 
@@ -790,6 +807,7 @@ int JdemHandle::step_async(long long n) {
   int bbox = any_free ? MODE_BBOX : 0;
   if (any_free) launch_bbox_reset(b, stream);  // stream-ordered: no host round trip
   launch_pre(dim, b, n == 1 ? bbox : 0, stream);
+  if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
   JDEM_CUDA_TRY(this, cudaGetLastError());
   // steps 1 .. n-1 run MODE_STEP (their epilogue starts the next step);
   // step n-1 also records the free-domain box; step n is MODE_STEP_LAST.
@@ -805,7 +823,8 @@ int JdemHandle::step_async(long long n) {
   if (any_free && mid > 0)
     if ((rc = run_graph(1, MODE_STEP | MODE_BBOX))) return rc;
   if ((rc = run_graph(1, MODE_STEP_LAST))) return rc;
-  if (rot_active) {
+  // Cundall-Strack integrates the rotation every step (k_cs_step)
+  if (rot_active && b.law != LAW_CS) {
     launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
     JDEM_CUDA_TRY(this, cudaGetLastError());
   }
@@ -876,6 +895,7 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
   }
   JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[0], stream));
   launch_pre(dim, b, 0, stream);
+  if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
   for (long long k = 0; k < n; ++k) {
     launch_rebuild(dim, b, any_free, stream);
     launch_nlbuild(dim, b, stream);
@@ -884,7 +904,7 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
     JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[3 + 2 * k], stream));
     launch_fin(b, true, false, 0, stream);
   }
-  if (rot_active) launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
+  if (rot_active && b.law != LAW_CS) launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
   JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[1], stream));
   JDEM_CUDA_TRY(this, cudaGetLastError());
   JDEM_CUDA_TRY(this, cudaEventSynchronize(ev_pool[1]));
@@ -930,7 +950,8 @@ int JdemHandle::compute_force() {
   launch_nlbuild(dim, b, stream);
   launch_force(dim, b, MODE_FORCE_ONLY, stream);
   int ad = dim == 3 ? 3 : 1;
-  JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));
+  // smooth-sphere laws exert no torque; Cundall-Strack wrote its own
+  if (b.law != LAW_CS) JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));
   JDEM_CUDA_TRY(this, cudaGetLastError());
   return sync_status();
 }

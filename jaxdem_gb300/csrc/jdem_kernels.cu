@@ -14,6 +14,7 @@
 #include "jdem_device.cuh"
 #include "jdem_kernels.h"
 #include "jdem_pair.cuh"
+#include "jdem_rot.cuh"
 
 namespace jdem {
 
@@ -546,43 +547,6 @@ __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
 // VelocityVerletSpiral: velocity_verlet_spiral.py:83-116, 156-180.
 // Spiral: spiral.py (step_after_force).  omega_dot: spiral.py:22-40.
 template <int DIM>
-__device__ __forceinline__ void omega_dot3(const float* w, const float* tq, const float* I,
-                                           const float* invI, float* out) {
-  if (DIM == 3) {
-    float cx = w[1] * (I[2] * w[2]) - w[2] * (I[1] * w[1]);
-    float cy = w[2] * (I[0] * w[0]) - w[0] * (I[2] * w[2]);
-    float cz = w[0] * (I[1] * w[1]) - w[1] * (I[0] * w[0]);
-    out[0] = (tq[0] - cx) * invI[0];
-    out[1] = (tq[1] - cy) * invI[1];
-    out[2] = (tq[2] - cz) * invI[2];
-  } else {
-    out[0] = tq[0] * invI[0];
-  }
-}
-
-template <int DIM>
-__device__ void ssprk3(float h, const float* w, const float* tq, const float* I, const float* invI,
-                       float fr, float* wout) {
-  constexpr int AD = DIM == 3 ? 3 : 1;
-  float k1[3], k2[3], k3[3], tmp[3];
-  omega_dot3<DIM>(w, tq, I, invI, k1);
-  for (int a = 0; a < AD; ++a) {
-    k1[a] = h * k1[a];
-    tmp[a] = w[a] + k1[a];
-  }
-  omega_dot3<DIM>(tmp, tq, I, invI, k2);
-  for (int a = 0; a < AD; ++a) {
-    k2[a] = h * k2[a];
-    tmp[a] = w[a] + 0.25f * (k1[a] + k2[a]);
-  }
-  omega_dot3<DIM>(tmp, tq, I, invI, k3);
-  for (int a = 0; a < AD; ++a) {
-    k3[a] = h * k3[a];
-    wout[a] = w[a] + fr * (k1[a] + k2[a] + 4.0f * k3[a]) / 6.0f;
-  }
-}
-
-template <int DIM>
 __global__ void k_rot(Bufs b, const int32_t* __restrict__ sys_of, float4* __restrict__ q,
                       float* __restrict__ angv, float* __restrict__ torque,
                       const float* __restrict__ inertia, const uint8_t* __restrict__ fixed,
@@ -603,79 +567,11 @@ __global__ void k_rot(Bufs b, const int32_t* __restrict__ sys_of, float4* __rest
   }
   float fr = fixed[i] ? 0.0f : 1.0f;
   for (long long s = 0; s < nsteps; ++s) {
-    if (domain == DOM_REFLECT) qq = q_unit(q_mul(make_float4(1.0f - 0.0f / 8.0f, 0.0f, 0.0f, 0.0f), qq));
-    if (rot == ROT_VVSPIRAL) {
-      float dt_2 = dt / 2.0f;
-      float wb[3], tb[3], wn[3];
-      if (DIM == 3) {
-        q_rotate3(qq, -1.0f, w, wb);
-        q_rotate3(qq, -1.0f, tq, tb);
-      } else {
-        wb[0] = w[0];
-        tb[0] = tq[0];
-      }
-      ssprk3<DIM>(dt_2, wb, tb, I, invI, fr, wn);
-      float rv[3];
-      if (DIM == 3) {
-        for (int a = 0; a < 3; ++a) rv[a] = 2.0f * dt_2 * wn[a];
-      } else {
-        float r = 2.0f * dt_2 * wn[0];
-        rv[0] = 0.0f * r;
-        rv[1] = 0.0f * r;
-        rv[2] = 1.0f * r;
-      }
-      float4 dq = q_small_rotvec(rv[0], rv[1], rv[2]);
-      qq = q_unit(q_mul(qq, dq));
-      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
-      else w[0] = wn[0];
-    }
+    if (domain == DOM_REFLECT) qq = reflect_q(qq);
+    rot_before<DIM>(rot, dt, qq, w, tq, I, invI, fr);
     // compute_force + ForceManager: torque = 0 + cross(0, F) + 0
     for (int a = 0; a < AD; ++a) tq[a] = 0.0f;
-    if (rot == ROT_VVSPIRAL) {
-      float dt_2 = dt / 2.0f;
-      float wb[3], tb[3] = {0, 0, 0}, wn[3];
-      if (DIM == 3) q_rotate3(qq, -1.0f, w, wb);
-      else wb[0] = w[0];
-      ssprk3<DIM>(dt_2, wb, tb, I, invI, fr, wn);
-      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
-      else w[0] = wn[0];
-    } else if (rot == ROT_SPIRAL) {
-      float dt_2 = dt / 2.0f;
-      float wb[3], tb[3] = {0, 0, 0}, wd[3], tmp[3], k1[3], k2[3], k3[3];
-      if (DIM == 3) q_rotate3(qq, -1.0f, w, wb);
-      else wb[0] = w[0];
-      omega_dot3<DIM>(wb, tb, I, invI, wd);
-      float rv1[3], rv2[3];
-      if (DIM == 3) {
-        for (int a = 0; a < 3; ++a) {
-          rv1[a] = 2.0f * dt_2 * wb[a];
-          rv2[a] = 2.0f * dt_2 * dt_2 * wd[a];
-        }
-      } else {
-        float r1 = 2.0f * dt_2 * wb[0], r2 = 2.0f * dt_2 * dt_2 * wd[0];
-        rv1[0] = 0.0f * r1; rv1[1] = 0.0f * r1; rv1[2] = 1.0f * r1;
-        rv2[0] = 0.0f * r2; rv2[1] = 0.0f * r2; rv2[2] = 1.0f * r2;
-      }
-      float4 dq = q_mul(q_small_rotvec(rv1[0], rv1[1], rv1[2]), q_small_rotvec(rv2[0], rv2[1], rv2[2]));
-      qq = q_unit(q_mul(qq, dq));
-      for (int a = 0; a < AD; ++a) {
-        k1[a] = dt * wd[a];
-        tmp[a] = wb[a] + k1[a];
-      }
-      omega_dot3<DIM>(tmp, tb, I, invI, k2);
-      for (int a = 0; a < AD; ++a) {
-        k2[a] = dt * k2[a];
-        tmp[a] = wb[a] + 0.25f * (k1[a] + k2[a]);
-      }
-      omega_dot3<DIM>(tmp, tb, I, invI, k3);
-      float wn[3];
-      for (int a = 0; a < AD; ++a) {
-        k3[a] = dt * k3[a];
-        wn[a] = wb[a] + fr * (k1[a] + k2[a] + 4.0f * k3[a]) / 6.0f;
-      }
-      if (DIM == 3) q_rotate3(qq, 1.0f, wn, w);
-      else w[0] = wn[0];
-    }
+    rot_after<DIM>(rot, dt, qq, w, nullptr, I, invI, fr);
   }
   q[i] = qq;
   for (int a = 0; a < AD; ++a) {
@@ -741,7 +637,16 @@ __global__ void k_energy(Bufs b, double* __restrict__ out) {
           int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
           float k = b.young[mat_i * b.n_mat + mat_j];
           float e;
-          if (b.law == LAW_HERTZ) {
+          if (b.law == LAW_CS) {
+            // CundallStrackForce.energy (cundall_strack.py:197-236): 0.5 kn delta^2,
+            // kn = 2 Ei Ri Ej Rj / (Ei Ri + Ej Rj), r = norm(r_ij)
+            const float Ei = b.mprop[mat_i * 4], Ej = b.mprop[mat_j * 4];
+            const float kn = (2.0f * Ei * pi.w * Ej * pj.w) / (Ei * pi.w + Ej * pj.w);
+            float r = dsq == 0.0f ? 0.0f : sqrtf(fmaxf(dsq, 1e-16f));
+            float s = R - r;
+            s = s > 0.0f ? s : 0.0f;
+            e = 0.5f * kn * (s * s);
+          } else if (b.law == LAW_HERTZ) {
             // HertzianForce.energy (hertz.py:149-160): r = norm(r_ij),
             // E = 0.4 k delta^(5/2), k = (4/3) E* sqrt(R*)
             float r = dsq == 0.0f ? 0.0f : sqrtf(fmaxf(dsq, 1e-16f));
@@ -1073,6 +978,10 @@ void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st) {
 
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
+  if (b.law == LAW_CS) {
+    launch_cs(dim, b, mode, st);
+    return;
+  }
   const bool gen = b.n_mat > 1 || (b.bond_w > 0 && !b.interact_same_bond);
   const unsigned int g = nblk(b.P, 128);
 #define JDEM_FORCE(D, L, G)                                                    \

@@ -22,6 +22,10 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
 int rebuild_kernel_count(bool any_free);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
+// Cundall-Strack (jdem_cs.cu): force + torque kernel, then the integrating
+// kernel unless mode is MODE_FORCE_ONLY; the rotational first-step phase.
+void launch_cs(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_cs_rot_pre(int dim, const Bufs& b, cudaStream_t st);
 void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st);
 // brick list build (jdem_tiles.cu)
 size_t tbuild_smem(int nst, int nv, int nrows);

@@ -1,8 +1,10 @@
 """Force model and force manager (``jaxdem/forces``).
 
-``SpringForce`` (``forces/spring.py:69-147``) and ``HertzianForce``
-(``forces/hertz.py:22-170``) are evaluated on the device by the collider
-kernels; these classes carry their identity and material requirements.  ``ForceManager`` (``forces/force_manager.py``) carries gravity
+``SpringForce`` (``forces/spring.py:69-147``), ``HertzianForce``
+(``forces/hertz.py:22-170``) and ``CundallStrackForce``
+(``forces/cundall_strack.py:22-242``) are evaluated on the device by the
+collider kernels; these classes carry their identity and material
+requirements.  ``ForceManager`` (``forces/force_manager.py``) carries gravity
 and the per-step external buffers; the device applies gravity
 (``force_manager.py:393-397``) inside the fused step kernel.
 """
@@ -61,6 +63,36 @@ def hertz_pair_constant(young, poisson) -> np.ndarray:
     with np.errstate(divide="ignore"):
         e_star = (F32(1.0) / (a[:, None] + a[None, :])).astype(F32)
     return (F32(4.0 / 3.0) * e_star).astype(F32)
+
+
+@ForceModel.register("cundallstrack")
+@dataclass
+class CundallStrackForce(ForceModel):
+    """Stateless Cundall-Strack spring-dashpot (``forces/cundall_strack.py:22-242``):
+    normal spring kn delta with viscous damping (strictly repulsive), tangential
+    dashpot capped by Coulomb friction, rolling-friction torque; per-material
+    ``young``, ``poisson``, ``e``, ``mu`` and ``mu_r``."""
+
+    @property
+    def required_material_properties(self) -> tuple:
+        return ("young", "poisson", "e", "mu", "mu_r")
+
+
+def cundall_strack_tables(young, poisson, e, mu, mu_r) -> tuple:
+    """Per-material-pair damping ratio beta (M, M) and per-material
+    (young, shear modulus, mu, mu_r) (M, 4), float32 in the reference's order
+    (``cundall_strack.py:128-150``): G = E / (2 (1 + nu)); e_eff = min(e_i, e_j);
+    beta = -ln(e_eff) / sqrt(pi**2 + ln(e_eff)**2), 1 where e_eff = 0."""
+    E = np.asarray(young, F32).reshape(-1)
+    nu = np.asarray(poisson, F32).reshape(-1)
+    G = (E / (F32(2.0) * (F32(1.0) + nu))).astype(F32)
+    ee = np.asarray(e, F32).reshape(-1)
+    e_eff = np.minimum(ee[:, None], ee[None, :])
+    e_safe = np.where(e_eff > 0, e_eff, F32(1.0)).astype(F32)
+    ln_e = np.log(e_safe).astype(F32)
+    beta = np.where(e_eff > 0, -ln_e / np.sqrt(F32(np.pi ** 2) + ln_e * ln_e), F32(1.0)).astype(F32)
+    props = np.stack([E, G, np.asarray(mu, F32).reshape(-1), np.asarray(mu_r, F32).reshape(-1)], 1)
+    return beta, np.ascontiguousarray(props, F32)
 
 
 @dataclass

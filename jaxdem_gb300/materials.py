@@ -36,6 +36,7 @@ class ElasticFriction(Material):
     mu: float
     e: float = 1.0
     density: float = 1.0
+    mu_r: float = 0.0  # rolling friction (materials/elastic_mats.py:45)
 
 
 class MaterialMatchmaker(Factory):

@@ -9,7 +9,7 @@ the result back (the functional contract of the reference API).
 
 Configurations outside the GB300 hot path raise ``NotImplementedError``:
 clumps (``pos_p != 0`` or shared ``clump_id``), facets, bonded force models,
-force models other than ``spring`` and ``hertz``, user force functions, pending external
+force models other than ``spring``, ``hertz`` and ``cundallstrack``, user force functions, pending external
 forces and user pre/post-step actions.
 """
 
@@ -39,7 +39,7 @@ def _domain_key(system) -> str:
 
 
 def _check_supported(state: State, system) -> None:
-    if system.force_model.type_name not in ("spring", "hertz"):
+    if system.force_model.type_name not in ("spring", "hertz", "cundallstrack"):
         raise NotImplementedError(f"force model '{system.force_model.type_name}' is not on the GB300 hot path")
     coll = system.collider.type_name
     if coll not in ("celllist", "naive", "celllistgb300", "neighborlist"):
@@ -111,34 +111,43 @@ def _skin(state: State, system) -> float:
 
 
 def pair_law(system) -> tuple:
-    """The force law's name and its (M, M) float32 pair constant: ``young_eff`` for
-    the spring, (4/3) E* for Hertz."""
+    """The force law's name, its (M, M) float32 pair constant (``young_eff`` for the
+    spring, (4/3) E* for Hertz, the damping ratio for Cundall-Strack) and the
+    per-material (M, 4) properties Cundall-Strack also needs (else None)."""
     law = system.force_model.type_name
+    mt = system.mat_table
     if law == "hertz":
         from .forces import hertz_pair_constant
 
-        return law, hertz_pair_constant(system.mat_table.young, system.mat_table.poisson)
-    return law, np.asarray(system.mat_table.young_eff, F32)
+        return law, hertz_pair_constant(mt.young, mt.poisson), None
+    if law == "cundallstrack":
+        from .forces import cundall_strack_tables
+
+        beta, props = cundall_strack_tables(mt.young, mt.poisson, mt.e, mt.mu, mt.mu_r)
+        return law, beta, props
+    return law, np.asarray(mt.young_eff, F32), None
 
 
 def engine_for(state: State, system) -> Engine:
     """Cached engine handle for this static configuration."""
     _check_supported(state, system)
     descs = _descs(state, system)
-    law, young = pair_law(system)
+    law, young, props = pair_law(system)
     W = _bond_width(state)
     skin = _skin(state, system)
     # a NeighborList collider's max_neighbors is the initial list capacity
     cap = getattr(system.collider, "max_neighbors", None)
     nl = int(cap) if cap else True
     key = (state.dim, W, bool(system.interact_same_bond_id), round(skin, 7), nl, law, young.tobytes(),
+           None if props is None else props.tobytes(),
            tuple((d["n"], d["domain"], d["linear"], d["rotation"], d["dt"], tuple(map(float, d["box_size"])),
                   tuple(map(float, d["anchor"])), d["restitution"], tuple(map(float, d["gravity"])),
                   d["cell_size"], d["search_range"]) for d in descs))
     eng = _CACHE.get(key)
     if eng is None:
         eng = Engine(state.dim, descs, young, skin=skin, bond_width=W,
-                     interact_same_bond_id=bool(system.interact_same_bond_id), neighbor_list=nl, force_law=law)
+                     interact_same_bond_id=bool(system.interact_same_bond_id), neighbor_list=nl, force_law=law,
+                     material_props=props)
         _CACHE[key] = eng
         while len(_CACHE) > _CACHE_MAX:
             _, old = _CACHE.popitem(last=False)
@@ -257,7 +266,8 @@ def rollout(state: State, system, strides: np.ndarray, save_fn: Callable):
     eng = engine_for(state, system)
     upload(eng, state)
     batched = state.batch_size > 1 and state.pos_c.ndim == 3
-    rot_static = _rotation_static(state)
+    # Cundall-Strack contacts exert torques: the rotational state always moves
+    rot_static = _rotation_static(state) and system.force_model.type_name != "cundallstrack"
     fields = ("pos_c", "vel", "force") if rot_static else Engine.FRAME_FIELDS
     free = system.domain.type_name == "free"
     fr = eng.rollout(strides, fields=fields, boxes=free)

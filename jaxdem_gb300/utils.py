@@ -66,7 +66,10 @@ def get_pair_forces_and_ids(state, system, cutoff=None, max_neighbors=None):
         d_sq = d_sq + rij[:, a] * rij[:, a]
     ri, rj = state.rad[i_ids], state.rad[sj]
     R = ri + rj
-    law, table = session.pair_law(system)
+    law, table, props = session.pair_law(system)
+    if law == "cundallstrack":
+        f = _cundall_strack_pairs(state, i_ids, sj, rij, table, props) * valid[:, None]
+        return state, system, np.column_stack((i_ids, j_ids)), f.astype(F32)
     k = table[state.mat_id[i_ids], state.mat_id[sj]]
     with np.errstate(divide="ignore", invalid="ignore"):
         inv = np.where(d_sq == 0, F32(0), F32(1) / np.sqrt(np.maximum(d_sq, F32(1e-16))))
@@ -81,6 +84,49 @@ def get_pair_forces_and_ids(state, system, cutoff=None, max_neighbors=None):
     else:
         f = ((k * delta * inv)[:, None] * rij).astype(F32) * valid[:, None]
     return state, system, np.column_stack((i_ids, j_ids)), f.astype(F32)
+
+
+def _cundall_strack_pairs(state, i, j, rij, beta, props):
+    """Contact force on i due to j of ``CundallStrackForce.force``
+    (``cundall_strack.py:100-196``) for the listed pairs, float32."""
+    d = rij.shape[1]
+    mi, mj = state.mat_id[i], state.mat_id[j]
+    Ei, Ej, Gi, Gj = props[mi, 0], props[mj, 0], props[mi, 1], props[mj, 1]
+    Ri, Rj = state.rad[i], state.rad[j]
+    m_i, m_j = state.mass[i], state.mass[j]
+    kn = (F32(2.0) * Ei * Ri * Ej * Rj) / (Ei * Ri + Ej * Rj)
+    kt = (F32(2.0) * Gi * Ri * Gj * Rj) / (Gi * Ri + Gj * Rj)
+    m_eff = (m_i * m_j) / (m_i + m_j)
+    mu_eff = np.minimum(props[mi, 2], props[mj, 2])
+    b = beta[mi, mj]
+    gamma_n = F32(2.0) * b * np.sqrt(kn * m_eff)
+    gamma_t = F32(2.0) * b * np.sqrt(kt * m_eff)
+
+    def unit_and_norm(v):
+        n2 = np.sum(v * v, axis=1, dtype=F32)
+        with np.errstate(divide="ignore"):
+            inv = np.where(n2 == 0, F32(0), F32(1) / np.sqrt(np.maximum(n2, F32(1e-16))))
+        return v * inv[:, None], n2 * inv
+
+    n, r = unit_and_norm(rij)
+    delta = Ri + Rj - r
+    contact = ((delta > 0) & (i != j)).astype(F32)
+    delta = delta * contact
+    w = np.asarray(state.ang_vel, F32)
+
+    def w_cross(wv, rv):
+        if d == 3:
+            return np.cross(wv, rv).astype(F32)
+        return np.stack([-wv[:, 0] * rv[:, 1], wv[:, 0] * rv[:, 0]], 1)
+
+    v_ci = state.vel[i] + w_cross(w[i], -Ri[:, None] * n)
+    v_cj = state.vel[j] + w_cross(w[j], Rj[:, None] * n)
+    v_rel = v_ci - v_cj
+    vn = np.sum(v_rel * n, axis=1, dtype=F32)
+    t, vt = unit_and_norm(v_rel - vn[:, None] * n)
+    Fn = np.maximum(F32(0), kn * delta - gamma_n * vn) * contact
+    Ft = np.minimum(gamma_t * vt, mu_eff * Fn) * contact
+    return (Fn[:, None] * n - Ft[:, None] * t).astype(F32)
 
 
 def grid_state(*, n_per_axis, spacing, radius: float = 1.0, mass: float = 1.0, jitter: float = 0.0,

@@ -94,7 +94,8 @@ class OSystem:
     time: np.floating = np.float32(0.0)
     step_count: int = 0
     inv_box_size: Optional[np.ndarray] = None
-    force_law: str = "spring"  # "spring" (forces/spring.py) | "hertz" (forces/hertz.py)
+    force_law: str = "spring"  # "spring" | "hertz" | "cundallstrack" (forces/*.py)
+    mat_props: Optional[np.ndarray] = None  # cundallstrack: (M, 4) young, shear modulus, mu, mu_r
 
     def __post_init__(self) -> None:
         if self.inv_box_size is None:
@@ -371,6 +372,109 @@ def hertz_energy_pair(i, j, pos, rad, mat_id, k43, sy: OSystem):
     return dt(0.4) * k * np.power(delta, dt(2.5))
 
 
+def cs_tables(young, poisson, e, mu, mu_r):
+    """``CundallStrackForce`` material terms (``forces/cundall_strack.py:128-150``):
+    the damping ratio beta (M, M) of e_eff = min(e_i, e_j) (1 where e_eff = 0) and
+    per material (young, G = E / (2 (1 + nu)), mu, mu_r) (M, 4), float32."""
+    f = np.float32
+    E = np.asarray(young, f).reshape(-1)
+    nu = np.asarray(poisson, f).reshape(-1)
+    G = E / (f(2.0) * (f(1.0) + nu))
+    ev = np.asarray(e, f).reshape(-1)
+    e_eff = np.minimum(ev[:, None], ev[None, :])
+    ln_e = np.log(np.where(e_eff > 0, e_eff, f(1.0))).astype(f)
+    beta = np.where(e_eff > 0, -ln_e / np.sqrt(f(np.pi ** 2) + ln_e ** 2), f(1.0)).astype(f)
+    props = np.stack([E, G, np.asarray(mu, f).reshape(-1), np.asarray(mu_r, f).reshape(-1)], 1).astype(f)
+    return beta, props
+
+
+def _unit_and_norm(v):
+    """``unit_and_norm`` (``utils/linalg.py:164-181``)."""
+    dt = v.dtype.type
+    n2 = sumsq(v)
+    with np.errstate(divide="ignore"):
+        inv = np.where(n2 == 0, dt(0), dt(1) / np.sqrt(np.maximum(n2, dt(1e-16))))
+    return v * inv[..., None], n2 * inv
+
+
+def _cross_w(w, r):
+    """``cross_3X3D_1X2D(w, r)`` (``utils/linalg.py:184-230``): w x r, 2D w = (0, 0, w_z)."""
+    if r.shape[-1] == 3:
+        return cross3(w, r)
+    return np.concatenate([-w * r[..., 1:2], w * r[..., 0:1]], axis=-1)
+
+
+def cs_pair(i, j, st, sy: OSystem):
+    """``CundallStrackForce.force`` (``forces/cundall_strack.py:100-196``), vectorised over
+    pairs: the force on ``i`` due to ``j`` and the torque on ``i``, concatenated
+    ``(..., dim + ang_dim)``."""
+    pos = st.pos_c
+    dt = pos.dtype.type
+    d = pos.shape[-1]
+    mi, mj = st.mat_id[i], st.mat_id[j]
+    P = sy.mat_props.astype(pos.dtype)
+    E_i, E_j, G_i, G_j = P[mi, 0], P[mj, 0], P[mi, 1], P[mj, 1]
+    R_i, R_j = st.rad[i], st.rad[j]
+    m_i, m_j = st.mass[i], st.mass[j]
+    kn = (dt(2.0) * E_i * R_i * E_j * R_j) / (E_i * R_i + E_j * R_j)
+    kt = (dt(2.0) * G_i * R_i * G_j * R_j) / (G_i * R_i + G_j * R_j)
+    m_eff = (m_i * m_j) / (m_i + m_j)
+    mu_eff = np.minimum(P[mi, 2], P[mj, 2])
+    beta = sy.young_eff.astype(pos.dtype)[mi, mj]
+    gamma_n = dt(2.0) * beta * np.sqrt(kn * m_eff)
+    gamma_t = dt(2.0) * beta * np.sqrt(kt * m_eff)
+    rij = displacement_fast(pos[i], pos[j], sy)
+    n, r = _unit_and_norm(rij)
+    delta = R_i + R_j - r
+    contact = ((delta > 0) & (np.asarray(i) != np.asarray(j))).astype(pos.dtype)
+    delta = delta * contact
+    r_ci = -R_i[..., None] * n
+    r_cj = R_j[..., None] * n
+    w = st.ang_vel
+    v_ci = st.vel[i] + _cross_w(w[i], r_ci)
+    v_cj = st.vel[j] + _cross_w(w[j], r_cj)
+    v_rel = v_ci - v_cj
+    vn = sumsq_dot(v_rel, n)
+    t, vt = _unit_and_norm(v_rel - vn[..., None] * n)
+    Fn = np.maximum(dt(0), kn * delta - gamma_n * vn) * contact
+    Ft = np.minimum(gamma_t * vt, mu_eff * Fn) * contact
+    F = Fn[..., None] * n - Ft[..., None] * t
+    if d == 3:
+        tq = cross3(r_ci, F)
+    else:
+        tq = r_ci[..., 0:1] * F[..., 1:2] - r_ci[..., 1:2] * F[..., 0:1]
+    mu_r = np.minimum(P[mi, 3], P[mj, 3])
+    R_eff = (R_i * R_j) / (R_i + R_j)
+    w_rel = w[i] - w[j]
+    n2 = sumsq(w_rel)
+    w_hat = w_rel * (dt(1) / np.sqrt(np.where(n2 == 0, dt(1), n2)))[..., None]
+    tq = tq - (mu_r * R_eff * Fn)[..., None] * w_hat
+    return np.concatenate([F, tq], axis=-1)
+
+
+def sumsq_dot(a, b):
+    """Left-to-right dot product along the last axis."""
+    acc = a[..., 0] * b[..., 0]
+    for k in range(1, a.shape[-1]):
+        acc = acc + a[..., k] * b[..., k]
+    return acc
+
+
+def cs_energy_pair(i, j, pos, rad, mat_id, sy: OSystem):
+    """``CundallStrackForce.energy`` (``forces/cundall_strack.py:197-236``): 0.5 kn delta^2."""
+    dt = pos.dtype.type
+    P = sy.mat_props.astype(pos.dtype)
+    E_i, E_j = P[mat_id[i], 0], P[mat_id[j], 0]
+    R_i, R_j = rad[i], rad[j]
+    kn = (dt(2.0) * E_i * R_i * E_j * R_j) / (E_i * R_i + E_j * R_j)
+    rij = displacement_fast(pos[i], pos[j], sy)
+    n2 = sumsq(rij)
+    r = np.where(n2 == 0, dt(0), np.sqrt(np.maximum(n2, dt(1e-16))))
+    delta = R_i + R_j - r
+    delta = delta * (delta > 0).astype(pos.dtype) * (np.asarray(i) != np.asarray(j)).astype(pos.dtype)
+    return dt(0.5) * kn * delta * delta
+
+
 def pair_force(i, j, pos, rad, mat_id, sy: OSystem):
     """The force law of ``sy`` (``System.force_model.force``)."""
     if sy.force_law == "hertz":
@@ -380,6 +484,8 @@ def pair_force(i, j, pos, rad, mat_id, sy: OSystem):
 
 def pair_energy(i, j, pos, rad, mat_id, sy: OSystem):
     """The force law's pair energy (``System.force_model.energy``)."""
+    if sy.force_law == "cundallstrack":
+        return cs_energy_pair(i, j, pos, rad, mat_id, sy)
     if sy.force_law == "hertz":
         return hertz_energy_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
     return spring_energy_pair(i, j, pos, rad, mat_id, sy.young_eff, sy)
@@ -440,6 +546,11 @@ def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     """
     pos = st.pos_c
     d = st.dim
+    if sy.force_law == "cundallstrack":
+        # force and torque summed together; torque + cross(pos_p = 0, F) (cell_list.py:452-464)
+        ad = st.torque.shape[-1]
+        ft = _traverse(st, sy, lambda i, j: cs_pair(i, j, st, sy), (d + ad,), pos.dtype, sum_dtype)
+        return ft[:, :d].astype(pos.dtype), ft[:, d:].astype(pos.dtype)
 
     def pair(i, j):
         return pair_force(i, j, pos, st.rad, st.mat_id, sy)
@@ -750,7 +861,7 @@ def step_once(st: OState, sy: OSystem, sum_dtype=None, collider="celllist"):
         st = vv_before(st, sy)
     if sy.rotation == "verletspiral":
         st = vvspiral_before(st, sy)
-    if collider == "naive":
+    if collider == "naive" and sy.force_law != "cundallstrack":
         st.force = naive_force(st, sy)
         st.torque = np.zeros_like(st.torque)
     else:

@@ -129,13 +129,35 @@ def test_hertz_force_model_pair_constant():
     st = jdem.State.create(pos=np.zeros((2, 3)), mat_table=table)
     sy = jdem.System.create(state=st, mat_table=table, force_model_type="hertz")
     assert type(sy.force_model).__name__ == "HertzianForce"
-    law, k = session.pair_law(sy)
-    assert law == "hertz" and k.dtype == F32
+    law, k, props = session.pair_law(sy)
+    assert law == "hertz" and k.dtype == F32 and props is None
     assert np.array_equal(k, R.hertz_constant([1e3, 4e3], [0.3, 0.2]))
     e_star = 1.0 / ((1 - 0.09) / 1e3 + (1 - 0.04) / 4e3)
     assert np.isclose(k[0, 1], 4.0 / 3.0 * e_star, rtol=1e-6) and k[0, 1] == k[1, 0]
-    law, k = session.pair_law(jdem.System.create(state=st, mat_table=table))
+    law, k, _ = session.pair_law(jdem.System.create(state=st, mat_table=table))
     assert law == "spring" and np.array_equal(k, table.young_eff)
+
+
+def test_cundall_strack_material_tables():
+    """CundallStrackForce (forces/cundall_strack.py:22-242) reads young, poisson, e, mu and
+    mu_r per material (elasticfrict, materials/elastic_mats.py:29-47); the engine gets the
+    damping ratio per material pair and (young, G, mu, mu_r) per material, equal to the
+    oracle's independent restatement bit for bit."""
+    from jaxdem_gb300 import session
+    from oracle import dem_ref as R
+
+    mats = [jdem.Material.create("elasticfrict", young=1e3, poisson=0.25, e=0.6, mu=0.4, mu_r=0.05),
+            jdem.Material.create("elasticfrict", young=3e3, poisson=0.3, e=0.0, mu=0.3)]
+    table = jdem.MaterialTable.from_materials(mats)
+    st = jdem.State.create(pos=np.zeros((2, 3)), mat_table=table, mat_id=[0, 1])
+    sy = jdem.System.create(state=st, mat_table=table, force_model_type="cundallstrack")
+    assert type(sy.force_model).__name__ == "CundallStrackForce"
+    law, beta, props = session.pair_law(sy)
+    rb, rp = R.cs_tables([1e3, 3e3], [0.25, 0.3], [0.6, 0.0], [0.4, 0.3], [0.05, 0.0])
+    assert law == "cundallstrack" and np.array_equal(beta, rb) and np.array_equal(props, rp)
+    # e = 0 takes the analytic limit beta = 1 (no NaN); G = E / (2 (1 + nu))
+    assert beta[1, 1] == 1.0 and beta[0, 1] == 1.0 and np.isfinite(beta).all()
+    assert np.isclose(props[0, 1], 1e3 / 2.5) and np.isclose(beta[0, 0], -np.log(0.6) / np.sqrt(np.pi ** 2 + np.log(0.6) ** 2))
 
 
 def test_rollout_frame_times_match_stepwise_float32():

@@ -12,7 +12,9 @@ analytic cases, on the numpy and C restatements:
   against the closed form, relative error < 1e-4;
 * two overlapping spheres (|F| = k delta), a periodic image pair, a wall bounce;
 * the Hertz law (no reference test covers it): two spheres against the closed
-  form, F = -dE/dd, and the C restatement against numpy.
+  form, F = -dE/dd, and the C restatement against numpy;
+* the Cundall-Strack law (no reference test covers it either): damping, sliding
+  friction below and at the Coulomb cap, torques, rolling friction, 2D and 3D.
 """
 
 from __future__ import annotations
@@ -128,6 +130,89 @@ def test_hertz_c_restatement_matches_numpy():
                         cell_size=float(sy.cell_size), young=k43, mat_id=mat, acc64=True, law="hertz")
     scale = np.abs(f).max()
     assert scale > 0 and np.abs(f - fc).max() <= 1e-6 * scale
+
+
+def _cs_sys(st, e=0.5, mu=0.4, mu_r=0.0, young=1e3, poisson=0.25, dtype=np.float64):
+    sy = _sys(3, domain="free", rad=st.rad, dtype=dtype)
+    beta, props = R.cs_tables([young], [poisson], [e], [mu], [mu_r])
+    sy.young_eff, sy.mat_props, sy.force_law = beta.astype(dtype), props.astype(dtype), "cundallstrack"
+    return sy
+
+
+def test_cundall_strack_closed_forms():
+    """Cundall-Strack (forces/cundall_strack.py:22-242), hand-derived on two equal spheres
+    (radius R, mass m, one material; no reference test covers the law):
+    kn = E R, m_eff = m / 2, beta = -ln e / sqrt(pi^2 + ln^2 e), gamma = 2 beta sqrt(k m_eff);
+    head-on approach: F = (kn delta - gamma_n vn) n; sliding: a tangential force of
+    min(gamma_t |v_t|, mu Fn) against the slip and a torque R Ft about n x t; e = 1: no
+    damping; rolling friction: a torque mu_r R_eff Fn against the relative spin."""
+    E, nu, Rr, m, e, mu = 1e3, 0.25, 0.5, 2.0, 0.5, 0.4
+    G = E / (2 * (1 + nu))
+    beta = -np.log(e) / np.sqrt(np.pi ** 2 + np.log(e) ** 2)
+    # the material tables are float32 (as in the reference): compare to 1e-6
+    kn, kt, m_eff = E * Rr, G * Rr, m / 2
+    gn, gt = 2 * beta * np.sqrt(kn * m_eff), 2 * beta * np.sqrt(kt * m_eff)
+    d, delta = 0.9, 0.1
+
+    def state(vel, w=None):
+        st = R.make_state(np.array([[0.0, 0, 0], [-d, 0, 0]]), rad=[Rr, Rr], mass=[m, m],
+                          vel=np.asarray(vel, float), dtype=np.float64)
+        if w is not None:
+            st.ang_vel = np.asarray(w, np.float64)
+        return st
+
+    # head-on: i moves towards j at 0.3 (n = +x points from j to i, vn = -0.3)
+    st = state([[-0.3, 0, 0], [0, 0, 0]])
+    f, t = R.cell_list_force(st, _cs_sys(st))
+    assert np.allclose(f[0], [kn * delta + gn * 0.3, 0, 0], rtol=1e-6)
+    assert np.allclose(f[1], -f[0], rtol=1e-6) and not np.any(t)
+    # sliding along y at 0.2: dashpot below the Coulomb cap, torque about z
+    st = state([[0, 0.2, 0], [0, 0, 0]])
+    f, t = R.cell_list_force(st, _cs_sys(st, mu=10.0))
+    ft = gt * 0.2
+    assert np.allclose(f[0], [kn * delta, -ft, 0], rtol=1e-6)
+    # r_ci = -R n = (-R, 0, 0); torque = r_ci x F = (0, 0, R ft)
+    assert np.allclose(t[0], [0, 0, Rr * ft], rtol=1e-6)
+    # a fast slide saturates at mu Fn
+    st = state([[0, 50.0, 0], [0, 0, 0]])
+    f, _ = R.cell_list_force(st, _cs_sys(st))
+    assert np.isclose(-f[0, 1], mu * kn * delta, rtol=1e-6)
+    # e = 1: no damping at all, the spring of stiffness kn remains
+    st = state([[-0.3, 0.2, 0], [0, 0, 0]])
+    f, _ = R.cell_list_force(st, _cs_sys(st, e=1.0))
+    assert np.allclose(f[0], [kn * delta, 0, 0], atol=1e-9)
+    # rolling friction opposes the relative spin about n (which adds no contact-point slip)
+    st = state([[0, 0, 0], [0, 0, 0]], w=[[3.0, 0, 0], [0, 0, 0]])
+    _, t = R.cell_list_force(st, _cs_sys(st, mu_r=0.2))
+    assert np.allclose(t[0], [-0.2 * (Rr / 2) * kn * delta, 0, 0], rtol=1e-6)
+    # energy 0.5 kn delta^2 per pair
+    assert np.isclose(R.cell_list_energy(st, _cs_sys(st)), 0.5 * kn * delta ** 2, rtol=1e-6)
+
+
+def test_cundall_strack_spin_slip_and_2d():
+    """A spinning sphere on a resting one: the contact point of i moves at w x r_ci, so a
+    spin about z of i slides the contact along -y (3D); in 2D the same contact gives the
+    scalar torque, and the float32 oracle follows the float64 one."""
+    E, Rr, m = 1e3, 0.5, 2.0
+    for dim in (3, 2):
+        pos = np.array([[0.0] * dim, [-0.9] + [0.0] * (dim - 1)])
+        w = np.zeros((2, 3 if dim == 3 else 1))
+        w[0, -1] = 2.0
+        out = {}
+        for dtype in (np.float64, F32):
+            st = R.make_state(pos, rad=[Rr, Rr], mass=[m, m], dtype=dtype)
+            st.ang_vel = w.astype(dtype)
+            sy = _sys(dim, domain="free", rad=st.rad, dtype=dtype)
+            beta, props = R.cs_tables([E], [0.25], [0.5], [10.0], [0.0])
+            sy.young_eff, sy.mat_props, sy.force_law = beta.astype(dtype), props.astype(dtype), "cundallstrack"
+            out[dtype] = R.cell_list_force(st, sy)
+        f, t = out[np.float64]
+        # w x r_ci with r_ci = (-R, 0) and w = 2 e_z: (0, -2R); friction acts along +y
+        assert f[0, 1] > 0 and np.isclose(f[0, 1], -f[1, 1])
+        # torque on i: r_ci x F = -R * F_y about z, opposing the spin
+        assert np.isclose(t[0, -1], -Rr * f[0, 1], rtol=1e-9) and t[0, -1] < 0
+        f32, t32 = out[F32]
+        assert np.allclose(f32, f, rtol=1e-5, atol=1e-6) and np.allclose(t32, t, rtol=1e-5, atol=1e-6)
 
 
 def test_periodic_image_pair():
