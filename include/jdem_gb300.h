@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 3
+#define JDEM_ABI_VERSION 4
 
 enum {
   JDEM_OK = 0,
@@ -105,7 +105,11 @@ typedef struct {
 /* Particle arrays in the reference layout.  Upload reads every field that is
  * not NULL (rad, mass are required; q/ang_vel/torque/inertia/mat_id/fixed/
  * bond_id default to identity/zero/State.create defaults when NULL).
- * Download writes pos_c, vel, force, q, ang_vel, torque when not NULL. */
+ * Download writes pos_c, vel, force, q, ang_vel, torque when not NULL.
+ * Rigid clumps (State.add_clump, state.py:1230-1420): pos_p (N, dim) holds each
+ * sphere's body-frame offset and clump_id (N) the clump index within its
+ * system; members store their clump's pos_c, vel, q, ang_vel, mass and
+ * inertia.  NULL for both means every sphere is its own body. */
 typedef struct {
   float* pos_c;
   float* vel;
@@ -119,6 +123,8 @@ typedef struct {
   int32_t* mat_id;
   uint8_t* fixed;
   int32_t* bond_id;
+  float* pos_p;
+  int32_t* clump_id;
 } JdemHostState;
 
 typedef struct {

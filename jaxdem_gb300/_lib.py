@@ -93,6 +93,8 @@ class HostState(C.Structure):
         ("mat_id", C.c_void_p),
         ("fixed", C.c_void_p),
         ("bond_id", C.c_void_p),
+        ("pos_p", C.c_void_p),
+        ("clump_id", C.c_void_p),
     ]
 
 
@@ -282,8 +284,10 @@ class Engine:
 
     # -- state transfer -------------------------------------------------
     def upload(self, pos, rad, mass, vel=None, force=None, q=None, ang_vel=None, torque=None,
-               inertia=None, mat_id=None, fixed=None, bond_id=None) -> None:
-        """Copy one State (concatenated systems) to the device."""
+               inertia=None, mat_id=None, fixed=None, bond_id=None, pos_p=None, clump_id=None) -> None:
+        """Copy one State (concatenated systems) to the device.  Rigid clumps: ``pos_p``
+        (body-frame offsets) and ``clump_id`` (clump index within each system); members
+        carry their clump's pos_c, vel, q, ang_vel, mass and inertia."""
         P, d = self.P, self.dim
         ad = 3 if d == 3 else 1
         keep = []
@@ -309,6 +313,8 @@ class Engine:
         hs.fixed = _ptr(arr(None if fixed is None else np.asarray(fixed).astype(np.uint8), np.uint8, (P,)))
         if self.bond_width > 0:
             hs.bond_id = _ptr(arr(bond_id, np.int32, (P, self.bond_width)))
+        hs.pos_p = _ptr(arr(pos_p, np.float32, (P, d)))
+        hs.clump_id = _ptr(arr(clump_id, np.int32, (P,)))
         self._check(self.lib.jdem_upload(self.h, C.byref(hs)))
 
     def download(self, out: Optional[dict] = None) -> dict:

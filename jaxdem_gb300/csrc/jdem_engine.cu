@@ -554,6 +554,25 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
       JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_bond, s->bond_id, N * bond_w * 4, kind, stream));
     }
   }
+  if (N) {
+    // rotational state in caller order; defaults on the device
+    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, s->q, N * 16, kind, stream));
+    else launch_identity_q((float4*)d_q, (long long)N, stream);
+    if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_w, s->ang_vel, N * ad * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
+    if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tq, s->torque, N * ad * 4, kind, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
+    if (s->inertia) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, s->inertia, N * ad * 4, kind, stream));
+    else launch_default_inertia(dim, (long long)N, st_mass, st_rad, d_inertia, stream);
+    // rigid clumps: the clumps' state from their members, and the members'
+    // world positions in place of pos_c for everything that follows
+    if ((rc = setup_clumps(s, device_ptrs))) return rc;
+    if (b.NC) {
+      launch_rb_init(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, (const float4*)d_q, d_w, d_tq, d_inertia,
+                     st_fixed, st_sys, st_pos, stream);
+      JDEM_CUDA_TRY(this, cudaGetLastError());
+    }
+  }
   // per-system maximum radius, bounding box and input checks, reduced on the
   // device (k_scan_input): the host reads eight words per system
   std::vector<float> rmax((size_t)S, 0.0f), lo((size_t)S * 3, 0.0f), hi((size_t)S * 3, 1.0f);
@@ -595,15 +614,6 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
   rc = plan_grid(rmax.data(), lo.data(), hi.data());
   if (rc) return rc;
   if (N) {
-    // rotational state in caller order; defaults on the device
-    if (s->q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_q, s->q, N * 16, kind, stream));
-    else launch_identity_q((float4*)d_q, (long long)N, stream);
-    if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_w, s->ang_vel, N * ad * 4, kind, stream));
-    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
-    if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tq, s->torque, N * ad * 4, kind, stream));
-    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
-    if (s->inertia) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_inertia, s->inertia, N * ad * 4, kind, stream));
-    else launch_default_inertia(dim, (long long)N, st_mass, st_rad, d_inertia, stream);
     // Is any rotational update non-trivial?  With omega = torque = 0 and
     // q = identity every rotation integrator and the reflect renormalisation
     // leave the state bit-identical, so the rotation kernel can be skipped.
@@ -675,6 +685,8 @@ int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const fl
     JDEM_CUDA_TRY(this, cudaMemsetAsync(d_inertia, 0, N * ad * 4, stream));
     launch_identity_q((float4*)d_q, (long long)N, stream);
     rot_active = false;
+    b.NC = 0;
+    b.sclump = nullptr;
     launch_pack(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, st_mat, st_fixed, st_sys, stream);
     JDEM_CUDA_TRY(this, cudaGetLastError());
   }
@@ -806,8 +818,13 @@ int JdemHandle::step_async(long long n) {
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
   int bbox = any_free ? MODE_BBOX : 0;
   if (any_free) launch_bbox_reset(b, stream);  // stream-ordered: no host round trip
-  launch_pre(dim, b, n == 1 ? bbox : 0, stream);
-  if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
+  rb_force_only = false;
+  if (b.NC) {
+    launch_rb_pre(dim, b, n == 1 ? bbox : 0, stream);
+  } else {
+    launch_pre(dim, b, n == 1 ? bbox : 0, stream);
+    if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
+  }
   JDEM_CUDA_TRY(this, cudaGetLastError());
   // steps 1 .. n-1 run MODE_STEP (their epilogue starts the next step);
   // step n-1 also records the free-domain box; step n is MODE_STEP_LAST.
@@ -823,8 +840,8 @@ int JdemHandle::step_async(long long n) {
   if (any_free && mid > 0)
     if ((rc = run_graph(1, MODE_STEP | MODE_BBOX))) return rc;
   if ((rc = run_graph(1, MODE_STEP_LAST))) return rc;
-  // Cundall-Strack integrates the rotation every step (k_cs_step)
-  if (rot_active && b.law != LAW_CS) {
+  // Cundall-Strack and rigid clumps integrate the rotation every step
+  if (rot_active && b.law != LAW_CS && !b.NC) {
     launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
     JDEM_CUDA_TRY(this, cudaGetLastError());
   }
@@ -894,8 +911,13 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
     return sync_status();
   }
   JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[0], stream));
-  launch_pre(dim, b, 0, stream);
-  if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
+  rb_force_only = false;
+  if (b.NC) {
+    launch_rb_pre(dim, b, 0, stream);
+  } else {
+    launch_pre(dim, b, 0, stream);
+    if (b.law == LAW_CS) launch_cs_rot_pre(dim, b, stream);
+  }
   for (long long k = 0; k < n; ++k) {
     launch_rebuild(dim, b, any_free, stream);
     launch_nlbuild(dim, b, stream);
@@ -904,7 +926,8 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
     JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[3 + 2 * k], stream));
     launch_fin(b, true, false, 0, stream);
   }
-  if (rot_active && b.law != LAW_CS) launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
+  if (rot_active && b.law != LAW_CS && !b.NC)
+    launch_rot(dim, b, st_sys, (float4*)d_q, d_w, d_tq, d_inertia, st_fixed, n, stream);
   JDEM_CUDA_TRY(this, cudaEventRecord(ev_pool[1], stream));
   JDEM_CUDA_TRY(this, cudaGetLastError());
   JDEM_CUDA_TRY(this, cudaEventSynchronize(ev_pool[1]));
@@ -930,7 +953,8 @@ int JdemHandle::download(JdemHostState* s, bool device_ptrs) {
   size_t N = (size_t)P;
   int ad = dim == 3 ? 3 : 1;
   if (N) {
-    launch_unpack(dim, b, st_pos, st_vel, st_frc, stream);
+    if (b.NC) launch_rb_unpack(dim, b, st_pos, st_vel, st_frc, (float4*)d_q, d_w, d_tq, rb_force_only, stream);
+    else launch_unpack(dim, b, st_pos, st_vel, st_frc, stream);
     JDEM_CUDA_TRY(this, cudaGetLastError());
     if (s->pos_c) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->pos_c, st_pos, N * dim * 4, kind, stream));
     if (s->vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->vel, st_vel, N * dim * 4, kind, stream));
@@ -950,8 +974,10 @@ int JdemHandle::compute_force() {
   launch_nlbuild(dim, b, stream);
   launch_force(dim, b, MODE_FORCE_ONLY, stream);
   int ad = dim == 3 ? 3 : 1;
-  // smooth-sphere laws exert no torque; Cundall-Strack wrote its own
-  if (b.law != LAW_CS) JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));
+  // smooth-sphere laws exert no torque; Cundall-Strack wrote its own, and
+  // rigid clumps keep each sphere's force and torque for the download
+  rb_force_only = b.NC > 0;
+  if (b.law != LAW_CS && !b.NC) JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, (size_t)P * ad * 4, stream));
   JDEM_CUDA_TRY(this, cudaGetLastError());
   return sync_status();
 }
@@ -970,6 +996,7 @@ int JdemHandle::energy(double* out, bool per_system) {
     if ((rc = dalloc((void**)&d_out, sizeof(double) * 4 * (size_t)P))) return rc;
     launch_energy(dim, b, d_out, stream);
     launch_ke_rot(dim, (long long)P, (const float4*)d_q, d_w, d_inertia, d_out + 3 * (size_t)P, stream);
+    if (b.NC) launch_rb_energy(dim, b, d_out, stream);  // the clumps' terms, once per clump
     JDEM_CUDA_TRY(this, cudaGetLastError());
     std::vector<double> h((size_t)P * 4);
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(h.data(), d_out, sizeof(double) * 4 * (size_t)P, cudaMemcpyDeviceToHost, stream));

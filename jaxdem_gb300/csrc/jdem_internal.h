@@ -61,6 +61,11 @@ struct JdemHandle {
   float4* d_q4 = nullptr;
   float *d_q = nullptr, *d_w = nullptr, *d_tq = nullptr, *d_inertia = nullptr;
 
+  // rigid clumps: device arrays sized for the clump / sphere counts of the
+  // last upload (b.NC = 0 when every sphere is its own body)
+  long long rb_cap_c = 0, rb_cap_p = 0;
+  int32_t* rb_sclump = nullptr;  // owner of b.sclump (b.sclump is null for sphere uploads)
+  bool rb_force_only = false;  // the last force evaluation was compute_force
   // trajectory frames (jdem_rollout): device slot ring and the copy stream
   // that drains it
   cudaStream_t copy_stream = nullptr;
@@ -117,5 +122,6 @@ struct JdemHandle {
   int neighbor_list(float cutoff, int max_neighbors, int32_t* out, int32_t* overflow);
   int domain_state(float* box, float* anchor);
   int rollout(const int64_t* strides, long long n_frames, const JdemFrames* out);
+  int setup_clumps(const JdemHostState* s, bool device_ptrs);
   void free_frames();
 };

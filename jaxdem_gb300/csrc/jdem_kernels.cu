@@ -634,6 +634,7 @@ __global__ void k_energy(Bufs b, double* __restrict__ out) {
             for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
             if (bonded) continue;
           }
+          if (b.sclump && b.sclump[oi] == b.sclump[b.orig[sel][j]]) continue;
           int mat_j = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
           float k = b.young[mat_i * b.n_mat + mat_j];
           float e;
@@ -693,8 +694,8 @@ __global__ void k_ke_rot(long long N, const float4* __restrict__ q, const float*
   out[i] = 0.5 * e;
 }
 
-// Canonical contacts: pairs with orig_i < orig_j and dsq < (ri + rj)^2,
-// evaluated with the same IEEE operations as the oracle.  Pass 0 counts per
+// Canonical contacts: pairs with orig_i < orig_j and dsq < (ri + rj)^2 (of
+// different clumps), evaluated with the same IEEE operations as the oracle.  Pass 0 counts per
 // slot, pass 1 writes (orig_i, orig_j) at the scanned offsets.
 template <int DIM>
 __global__ void k_contacts(Bufs b, int pass, int32_t* __restrict__ counts,
@@ -732,6 +733,8 @@ __global__ void k_contacts(Bufs b, int pass, int32_t* __restrict__ counts,
         for (int j = b.cell_start[row + ca]; j < b.cell_start[row + cb]; ++j) {
           int oj = b.orig[sel][j];
           if (oj <= oi) continue;
+          // spheres of one rigid clump never interact
+          if (b.sclump && b.sclump[oi] == b.sclump[oj]) continue;
           float4 pj = P[j];
           float d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
           if (per)
@@ -978,6 +981,10 @@ void launch_cond(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st) {
 
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
+  if (b.NC) {
+    launch_rb(dim, b, mode, st);
+    return;
+  }
   if (b.law == LAW_CS) {
     launch_cs(dim, b, mode, st);
     return;

@@ -26,6 +26,15 @@ void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
 // kernel unless mode is MODE_FORCE_ONLY; the rotational first-step phase.
 void launch_cs(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_cs_rot_pre(int dim, const Bufs& b, cudaStream_t st);
+// Rigid clumps (jdem_rigid.cu)
+void launch_rb(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_rb_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
+void launch_rb_init(int dim, const Bufs& b, const float* pos, const float* vel, const float* frc, const float* rad,
+                    const float* mass, const float4* q, const float* angv, const float* torque, const float* inertia,
+                    const uint8_t* fixed, const int32_t* sys_of, float* world, cudaStream_t st);
+void launch_rb_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, float4* q, float* angv,
+                      float* torque, bool per_sphere, cudaStream_t st);
+void launch_rb_energy(int dim, const Bufs& b, double* out, cudaStream_t st);
 void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st);
 // brick list build (jdem_tiles.cu)
 size_t tbuild_smem(int nst, int nv, int nrows);

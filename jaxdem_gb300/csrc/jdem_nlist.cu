@@ -171,6 +171,7 @@ int JdemHandle::neighbor_list(float cutoff, int max_nb, int32_t* out, int32_t* o
   if (overflow) *overflow = 0;
   if (P == 0 || max_nb == 0) return JDEM_OK;
   if (!out) return fail(JDEM_ERR_BAD_ARG, "neighbor_list: null output");
+  if (b.NC) return fail(JDEM_ERR_UNSUPPORTED, "neighbor_list: rigid clumps are not supported");
   cudaSetDevice(dev);
   // Reference grid per system.
   std::vector<NlGrid> grids((size_t)S);

@@ -88,7 +88,7 @@ struct ContactSum {
   float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
   float4 pi;
   float k0;
-  int mat_i, oi;
+  int mat_i, oi, ci;
   bool per;
   const SysParams* sp;
 
@@ -98,7 +98,8 @@ struct ContactSum {
     per = s.domain == DOM_PERIODIC;
     mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
     k0 = b.young[mat_i * b.n_mat + mat_i];
-    oi = (GENERAL && b.bond_w > 0 && !b.interact_same_bond) ? b.orig[sel][t] : 0;
+    oi = (GENERAL && ((b.bond_w > 0 && !b.interact_same_bond) || b.sclump)) ? b.orig[sel][t] : 0;
+    ci = (GENERAL && b.sclump) ? b.sclump[oi] : 0;
   }
 
   // Adds the force on i due to j (position pj).  The slot j is read only for
@@ -124,6 +125,8 @@ struct ContactSum {
         for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
         if (bonded) return;
       }
+      // spheres of one rigid clump do not interact (clump_i != clump_j)
+      if (GENERAL && b.sclump && b.sclump[b.orig[sel][j]] == ci) return;
       contact(k, dsq, R, pj.w, dx, dy, dz);
     }
   }

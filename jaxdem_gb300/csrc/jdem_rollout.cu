@@ -198,8 +198,15 @@ int JdemHandle::rollout(const int64_t* strides, long long T, const JdemFrames* o
     if (slot == 0 || N == 0) continue;
     if (device_dst) {
       // frames stay in HBM: unpack straight into frame t
-      float* dp[3];
-      for (int k = 0; k < 3; ++k) dp[k] = f[k].dst ? f[k].dst + (size_t)t * N * dim : nullptr;
+      float* dp[6];
+      for (int k = 0; k < 6; ++k) dp[k] = f[k].dst ? (float*)((char*)f[k].dst + (size_t)t * f[k].bytes) : nullptr;
+      if (b.NC) {
+        // rigid clumps: every field from the clumps' state
+        launch_rb_unpack(dim, b, dp[0], dp[1], dp[2], (float4*)dp[3], dp[4], dp[5], false, stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return stop(fail(JDEM_ERR_CUDA, std::string("rollout unpack: ") + cudaGetErrorString(e)));
+        continue;
+      }
       if (dp[0] || dp[1] || dp[2]) launch_unpack(dim, b, dp[0], dp[1], dp[2], stream);
       for (int k = 3; k < 6; ++k)
         if (f[k].dst) {
@@ -219,11 +226,18 @@ int JdemHandle::rollout(const int64_t* strides, long long T, const JdemFrames* o
       if (e != cudaSuccess) return stop(fail(JDEM_ERR_CUDA, std::string("rollout: ") + cudaGetErrorString(e)));
     }
     char* ds = d_frames + (size_t)r * slot;
-    launch_unpack(dim, b, f[0].dst ? (float*)(ds + f[0].off) : nullptr, f[1].dst ? (float*)(ds + f[1].off) : nullptr,
-                  f[2].dst ? (float*)(ds + f[2].off) : nullptr, stream);
-    cudaError_t e = cudaGetLastError();
-    for (int k = 3; k < 6 && e == cudaSuccess; ++k)
-      if (f[k].dst) e = cudaMemcpyAsync(ds + f[k].off, rot_src[k - 3], f[k].bytes, cudaMemcpyDeviceToDevice, stream);
+    float* sp_[6];
+    for (int k = 0; k < 6; ++k) sp_[k] = f[k].dst ? (float*)(ds + f[k].off) : nullptr;
+    cudaError_t e;
+    if (b.NC) {
+      launch_rb_unpack(dim, b, sp_[0], sp_[1], sp_[2], (float4*)sp_[3], sp_[4], sp_[5], false, stream);
+      e = cudaGetLastError();
+    } else {
+      launch_unpack(dim, b, sp_[0], sp_[1], sp_[2], stream);
+      e = cudaGetLastError();
+      for (int k = 3; k < 6 && e == cudaSuccess; ++k)
+        if (f[k].dst) e = cudaMemcpyAsync(ds + f[k].off, rot_src[k - 3], f[k].bytes, cudaMemcpyDeviceToDevice, stream);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(ev_unpacked, stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(copy_stream, ev_unpacked, 0);
     // page-locked destinations are written by the copy engine while the host

@@ -8,7 +8,7 @@ captured CUDA graphs; each call uploads the caller's state, runs, and reads
 the result back (the functional contract of the reference API).
 
 Configurations outside the GB300 hot path raise ``NotImplementedError``:
-clumps (``pos_p != 0`` or shared ``clump_id``), facets, bonded force models,
+rigid clumps in a reflect domain or with Cundall-Strack contacts, facets, bonded force models,
 force models other than ``spring``, ``hertz`` and ``cundallstrack``, user force functions, pending external
 forces and user pre/post-step actions.
 """
@@ -60,14 +60,24 @@ def _check_supported(state: State, system) -> None:
 
     if system.user_pre_step_actions is not _save_state_system or system.user_post_step_actions is not _save_state_system:
         raise NotImplementedError("user pre/post step actions are outside the GB300 hot path")
-    if np.any(state.pos_p != 0):
-        raise NotImplementedError("clumps (pos_p != 0) are outside the GB300 hot path")
-    N = state.N
-    cid = state.clump_id.reshape(-1, N) if N else state.clump_id
-    if N and np.any(cid != np.arange(N)):
-        raise NotImplementedError("clumps (shared clump_id) are outside the GB300 hot path")
+    if _has_clumps(state):
+        if system.domain.type_name == "reflect":
+            raise NotImplementedError("rigid clumps in a reflect domain are not supported by the GB300 engine")
+        if system.force_model.type_name == "cundallstrack":
+            raise NotImplementedError("rigid clumps with Cundall-Strack contacts are not supported by the GB300 engine")
     if state.facet_id.size and np.any(state.facet_id != -1):
         raise NotImplementedError("facets are outside the GB300 hot path")
+
+
+def _has_clumps(state: State) -> bool:
+    """Rigid clumps: a body-frame offset, or a clump id shared by several spheres."""
+    N = state.N
+    if N == 0:
+        return False
+    if np.any(state.pos_p != 0):
+        return True
+    cid = state.clump_id.reshape(-1, N)
+    return bool(np.any(cid != np.arange(N)))
 
 
 def _per_batch(x, B: int, shape_tail: tuple) -> np.ndarray:
@@ -177,7 +187,9 @@ def upload(eng: Engine, state: State) -> None:
                q=_flat(state.q.as_array(), P, (4,)), ang_vel=_flat(state.ang_vel, P, (ad,)),
                torque=_flat(state.torque, P, (ad,)), inertia=_flat(state.inertia, P, (ad,)),
                mat_id=_flat(state.mat_id, P, ()), fixed=_flat(state.fixed, P, ()),
-               bond_id=None if W == 0 else _bond_global(state, W))
+               bond_id=None if W == 0 else _bond_global(state, W),
+               pos_p=_flat(state.pos_p, P, (d,)) if _has_clumps(state) else None,
+               clump_id=_flat(state.clump_id, P, ()) if _has_clumps(state) else None)
 
 
 def _bond_global(state: State, W: int) -> np.ndarray:
@@ -266,8 +278,9 @@ def rollout(state: State, system, strides: np.ndarray, save_fn: Callable):
     eng = engine_for(state, system)
     upload(eng, state)
     batched = state.batch_size > 1 and state.pos_c.ndim == 3
-    # Cundall-Strack contacts exert torques: the rotational state always moves
-    rot_static = _rotation_static(state) and system.force_model.type_name != "cundallstrack"
+    # Cundall-Strack contacts and rigid clumps exert torques: the rotational state moves
+    rot_static = (_rotation_static(state) and system.force_model.type_name != "cundallstrack"
+                  and not _has_clumps(state))
     fields = ("pos_c", "vel", "force") if rot_static else Engine.FRAME_FIELDS
     free = system.domain.type_name == "free"
     fr = eng.rollout(strides, fields=fields, boxes=free)

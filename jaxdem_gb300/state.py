@@ -195,6 +195,80 @@ class State:
                      mat_id=mat_id, species_id=species_id, fixed=fixed, facet_id=facet_id)
 
     @staticmethod
+    def merge(a: "State", b: "State") -> "State":
+        """Concatenate two unbatched states along the particle axis (``state.py:868-975``):
+        the second state's clump ids are shifted past the first's, its bond indices by
+        the first's particle count."""
+        kw = {}
+        na = a.N
+        for f in fields(a):
+            va, vb = getattr(a, f.name), getattr(b, f.name)
+            if isinstance(va, Quaternion):
+                kw[f.name] = Quaternion(np.concatenate([va.w, vb.w]), np.concatenate([va.xyz, vb.xyz]))
+            elif f.name == "clump_id":
+                off = int(va.max()) + 1 if va.size else 0
+                kw[f.name] = np.concatenate([va, vb + off]).astype(np.int32)
+            elif f.name == "bond_id":
+                w = max(va.shape[-1], vb.shape[-1])
+                pa = np.pad(va, ((0, 0), (0, w - va.shape[-1])), constant_values=-1)
+                pb = np.pad(np.where(vb >= 0, vb + na, -1), ((0, 0), (0, w - vb.shape[-1])), constant_values=-1)
+                kw[f.name] = np.concatenate([pa, pb]).astype(np.int32)
+            elif f.name == "facet_id" and va.shape[:1] != (na,):
+                kw[f.name] = va
+            else:
+                kw[f.name] = np.concatenate([va, vb])
+        return State(**kw)
+
+    @staticmethod
+    def add_clump(state: "State", pos, *, pos_p=None, vel=None, force=None, q=None, ang_vel=None, torque=None,
+                  rad=None, volume=None, mass=None, inertia=None, bond_id=None, mat_id=None, species_id=None,
+                  fixed=None) -> "State":
+        """``State.add_clump`` (``state.py:1230-1420``): append one rigid clump.
+
+        With ``pos_p`` None, ``pos`` are the spheres' absolute positions and the
+        centre is their volume-weighted mean (offsets rotated back by ``q`` when
+        given); otherwise ``pos`` is the centre and ``pos_p`` the body-frame
+        offsets.  The clump's velocity, orientation, spin, mass, inertia and
+        fixed flag are broadcast to every member (members store the clump's
+        totals)."""
+        pos = np.asarray(pos, F32)
+        d = pos.shape[-1]
+        ad = 1 if d == 2 else 3
+        qobj = None
+        if q is not None:
+            qobj = q if isinstance(q, Quaternion) else Quaternion.from_array(np.asarray(q, F32))
+        if pos_p is None:
+            n_new = pos.shape[-2]
+            rad_arr = np.ones(n_new, F32) if rad is None else np.asarray(rad, F32)
+            vol = _hypersphere_volume(rad_arr, d)
+            vsum = vol.sum(dtype=F32)
+            com = (pos * vol[:, None]).sum(axis=0, dtype=F32) / (F32(1.0) if vsum == 0 else vsum)
+            pos_c = np.broadcast_to(com.astype(F32), pos.shape).copy()
+            raw = (pos - pos_c).astype(F32)
+            if qobj is not None:
+                qb = Quaternion(np.broadcast_to(qobj.w, (n_new, 1)).copy(), np.broadcast_to(qobj.xyz, (n_new, 3)).copy())
+                pos_p = _rotate(Quaternion(qb.w, -qb.xyz), raw)
+            else:
+                pos_p = raw
+        else:
+            pos_p = np.asarray(pos_p, F32)
+            n_new = pos_p.shape[-2]
+            com = pos if pos.ndim == 1 else pos[0]
+            pos_c = np.broadcast_to(np.asarray(com, F32), (n_new, d)).copy()
+
+        def bc(v, shape, dt=F32):
+            return None if v is None else np.broadcast_to(np.asarray(v, dt), shape).copy()
+
+        if qobj is not None:
+            qobj = Quaternion(np.broadcast_to(qobj.w, (n_new, 1)).copy(), np.broadcast_to(qobj.xyz, (n_new, 3)).copy())
+        new = State.create(pos=pos_c, pos_p=pos_p, vel=bc(vel, (n_new, d)), force=bc(force, (n_new, d)), q=qobj,
+                           ang_vel=bc(ang_vel, (n_new, ad)), torque=bc(torque, (n_new, ad)), rad=rad,
+                           volume=bc(volume, (n_new,)), mass=bc(mass, (n_new,)), inertia=bc(inertia, (n_new, ad)),
+                           clump_id=np.zeros(n_new, np.int32), bond_id=bond_id, mat_id=bc(mat_id, (n_new,), np.int32),
+                           species_id=bc(species_id, (n_new,), np.int32), fixed=bc(fixed, (n_new,), bool))
+        return State.merge(state, new)
+
+    @staticmethod
     def stack(states: Sequence["State"]) -> "State":
         """Stack along a new leading axis (``state.py:1131-1203``)."""
         kw = {}

@@ -46,7 +46,8 @@ PAIR_UNROLL = 4  # colliders/cell_list.py:184
 
 @dataclass
 class OState:
-    """Particle record, fields as ``State`` (``state.py:103-228``), spheres only."""
+    """Particle record, fields as ``State`` (``state.py:103-228``): spheres, or rigid
+    clumps whose members store the clump's pos_c, vel, q, ang_vel, mass and inertia."""
 
     pos_c: np.ndarray  # (N, d)
     vel: np.ndarray  # (N, d)
@@ -61,6 +62,7 @@ class OState:
     fixed: np.ndarray  # (N,) bool
     bond_id: np.ndarray  # (N, W) int, -1 padded
     clump_id: np.ndarray  # (N,) int
+    pos_p: Optional[np.ndarray] = None  # (N, d) body-frame offsets of rigid-clump members
 
     @property
     def N(self) -> int:
@@ -71,7 +73,14 @@ class OState:
         return self.pos_c.shape[1]
 
     def copy(self) -> "OState":
-        return OState(**{k: np.array(v, copy=True) for k, v in self.__dict__.items()})
+        return OState(**{k: None if v is None else np.array(v, copy=True) for k, v in self.__dict__.items()})
+
+    @property
+    def rigid(self) -> bool:
+        """Rigid clumps present (an offset, or a clump id shared by several spheres)."""
+        if self.pos_p is not None and np.any(self.pos_p != 0):
+            return True
+        return bool(np.any(self.clump_id != np.arange(self.N)))
 
 
 @dataclass
@@ -108,7 +117,7 @@ class OSystem:
 
 def make_state(pos, vel=None, rad=None, mass=None, density=None, mat_id=None,
                fixed=None, bond_id=None, ang_vel=None, torque=None, q=None,
-               force=None, dtype=np.float32) -> OState:
+               force=None, dtype=np.float32, pos_p=None, clump_id=None, inertia=None) -> OState:
     """Defaults of ``State.create`` (``state.py:640-862``) for spheres."""
     pos = np.asarray(pos, dtype)
     N, d = pos.shape
@@ -122,7 +131,10 @@ def make_state(pos, vel=None, rad=None, mass=None, density=None, mat_id=None,
     mass = np.ones(N, dtype) if mass is None else np.asarray(mass, dtype)
     ang_vel = np.zeros((N, ad), dtype) if ang_vel is None else np.asarray(ang_vel, dtype).reshape(N, ad)
     coeff = dtype(0.5) if d == 2 else dtype(0.4)
-    inertia = ((coeff * mass) * rad * rad)[:, None] * np.ones((N, ad), dtype)  # state.py:817-823
+    if inertia is None:
+        inertia = ((coeff * mass) * rad * rad)[:, None] * np.ones((N, ad), dtype)  # state.py:817-823
+    else:
+        inertia = np.asarray(inertia, dtype).reshape(N, ad).copy()
     if q is None:
         q = np.zeros((N, 4), dtype)
         q[:, 0] = 1
@@ -139,7 +151,8 @@ def make_state(pos, vel=None, rad=None, mass=None, density=None, mat_id=None,
         mat_id=mat_id,
         fixed=np.zeros(N, bool) if fixed is None else np.asarray(fixed, bool),
         bond_id=np.full((N, 1), -1, np.int64) if bond_id is None else np.asarray(bond_id, np.int64),
-        clump_id=np.arange(N, dtype=np.int64),
+        clump_id=np.arange(N, dtype=np.int64) if clump_id is None else np.asarray(clump_id, np.int64),
+        pos_p=np.zeros((N, d), dtype) if pos_p is None else np.asarray(pos_p, dtype).copy(),
     )
 
 
@@ -497,6 +510,20 @@ def valid_mask(clump_i, clump_j, bond_row_i, index_j, interact_same_bond_id):
     return (clump_i != clump_j) & ((~is_bonded) | bool(interact_same_bond_id))
 
 
+def pos_p_rot(st: OState):
+    """``state._pos_p_rot`` (``state.py:230-273``): R(q) pos_p, zero for spheres."""
+    if st.pos_p is None or not np.any(st.pos_p != 0):
+        return np.zeros_like(st.pos_c)
+    return quat_rotate(st.q, st.pos_p).astype(st.pos_c.dtype)
+
+
+def world_pos(st: OState):
+    """``State.pos`` (``state.py:295-304``): pos_c + R(q) pos_p."""
+    if st.pos_p is None or not np.any(st.pos_p != 0):
+        return st.pos_c
+    return st.pos_c + pos_p_rot(st)
+
+
 def _traverse(st: OState, sy: OSystem, pair_fn, acc_shape, acc_dtype, sum_dtype=None):
     """``_traverse_pairs`` (``colliders/cell_list.py:187-261``), vectorised over particles.
 
@@ -505,7 +532,7 @@ def _traverse(st: OState, sy: OSystem, pair_fn, acc_shape, acc_dtype, sum_dtype=
     float32 pair terms, used as the tighter force check).
     """
     N = st.N
-    pos = st.pos_c  # spheres: pos = pos_c + R(q)·0
+    pos = world_pos(st)
     sum_dtype = acc_dtype if sum_dtype is None else sum_dtype
     perm, sorted_h, nh = spatial_partition(pos, sy, sy.cell_size, sy.neighbor_mask)
     if sy.periodic:
@@ -542,9 +569,10 @@ def _traverse(st: OState, sy: OSystem, pair_fn, acc_shape, acc_dtype, sum_dtype=
 def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     """``DynamicCellList.compute_force`` (``colliders/cell_list.py:434-464``).
 
-    Returns ``(force, torque)``; torque is ``0 + cross(0, F) = 0`` for spheres.
+    Returns ``(force, torque)`` with torque = sum of pair torques + cross(R(q) pos_p, F):
+    ``0 + cross(0, F) = 0`` for smooth spheres.
     """
-    pos = st.pos_c
+    pos = world_pos(st)
     d = st.dim
     if sy.force_law == "cundallstrack":
         # force and torque summed together; torque + cross(pos_p = 0, F) (cell_list.py:452-464)
@@ -555,13 +583,21 @@ def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     def pair(i, j):
         return pair_force(i, j, pos, st.rad, st.mat_id, sy)
 
-    f = _traverse(st, sy, pair, (d,), pos.dtype, sum_dtype)
-    return f.astype(pos.dtype), np.zeros_like(st.torque)
+    f = _traverse(st, sy, pair, (d,), pos.dtype, sum_dtype).astype(pos.dtype)
+    if not st.rigid:
+        return f, np.zeros_like(st.torque)
+    r = pos_p_rot(st)
+    t = pos.dtype.type
+    if d == 3:
+        tq = t(0) + cross3(r, f)
+    else:
+        tq = t(0) + (r[:, 0:1] * f[:, 1:2] - r[:, 1:2] * f[:, 0:1])
+    return f, tq.astype(pos.dtype)
 
 
 def cell_list_energy(st: OState, sy: OSystem, sum_dtype=None):
     """``DynamicCellList.compute_potential_energy`` (``cell_list.py:466-496``), pair term x0.5 (``_partition.py:39-51``)."""
-    pos = st.pos_c
+    pos = world_pos(st)
     half = pos.dtype.type(0.5)
 
     def pair(i, j):
@@ -574,7 +610,7 @@ def cell_list_energy(st: OState, sy: OSystem, sum_dtype=None):
 def naive_force(st: OState, sy: OSystem, sum_dtype=np.float64):
     """``NaiveSimulator.compute_force`` (``colliders/naive.py:187-235``), O(N^2)."""
     N = st.N
-    pos = st.pos_c
+    pos = world_pos(st)
     iota = np.arange(N)
     out = np.zeros((N, st.dim), sum_dtype)
     for i in range(N):
@@ -619,6 +655,8 @@ def reflect_apply(st: OState, sy: OSystem):
     the identity, the rotational denominator and lever-arm terms vanish and
     ``count_active`` equals ``active``.
     """
+    if st.rigid:
+        raise NotImplementedError("the oracle's reflect domain is restated for spheres only")
     t = st.pos_c.dtype.type
     e = t(sy.restitution)
     pos = st.pos_c
@@ -655,8 +693,14 @@ def reflect_apply(st: OState, sy: OSystem):
 
 
 def free_apply(st: OState, sy: OSystem):
-    """``FreeDomain.apply`` (``domains/free.py:40-63``): bounding box of the spheres."""
-    rad = st.rad[:, None]
+    """``FreeDomain.apply`` (``domains/free.py:40-63``): the box of pos_c -+ (norm(pos_p) + rad)."""
+    t = st.pos_c.dtype.type
+    if st.rigid:
+        n2 = sumsq(st.pos_p)
+        nrm = np.where(n2 == 0, t(0), np.sqrt(np.maximum(n2, t(1e-16))))
+        rad = (nrm + st.rad)[:, None]
+    else:
+        rad = st.rad[:, None]
     p_min = np.min(st.pos_c - rad, axis=0)
     p_max = np.max(st.pos_c + rad, axis=0)
     sy.box_size = (p_max - p_min).astype(st.pos_c.dtype)
@@ -665,12 +709,24 @@ def free_apply(st: OState, sy: OSystem):
 
 
 def force_manager_apply(st: OState, sy: OSystem):
-    """``ForceManager.apply`` (``forces/force_manager.py:338-425``) for spheres (count == 1)."""
+    """``ForceManager.apply`` (``forces/force_manager.py:338-425``): contact + gravity *
+    (mass / count) per sphere, then the clump sums (``segment_sum`` over clump_id, members
+    added in index order) broadcast back to every member."""
     t = st.pos_c.dtype.type
-    F_com = sy.gravity.astype(st.pos_c.dtype) * (st.mass / t(1.0))[:, None]
+    count = np.bincount(st.clump_id, minlength=st.N)[st.clump_id].astype(st.pos_c.dtype)
+    F_com = sy.gravity.astype(st.pos_c.dtype) * (st.mass / count)[:, None]
     F_part = np.zeros_like(st.force)
-    st.force = st.force + F_part + F_com
-    st.torque = st.torque + np.zeros_like(st.torque)
+    F_total = st.force + F_part + F_com
+    T_total = st.torque + np.zeros_like(st.torque)
+    if not st.rigid:
+        st.force, st.torque = F_total, T_total
+        return st
+    F_c = np.zeros_like(F_total)
+    T_c = np.zeros_like(T_total)
+    for i in range(st.N):  # index order: the engine's member order
+        F_c[st.clump_id[i]] = F_c[st.clump_id[i]] + F_total[i]
+        T_c[st.clump_id[i]] = T_c[st.clump_id[i]] + T_total[i]
+    st.force, st.torque = F_c[st.clump_id], T_c[st.clump_id]
     return st
 
 
@@ -895,7 +951,7 @@ def naive_energy(st: OState, sy: OSystem) -> float:
     N = st.N
     ii, jj = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
     ii, jj = ii.ravel(), jj.ravel()
-    e = pair_energy(ii, jj, st.pos_c, st.rad, st.mat_id, sy)
+    e = pair_energy(ii, jj, world_pos(st), st.rad, st.mat_id, sy)
     ok = valid_mask(st.clump_id[ii], st.clump_id[jj], st.bond_id[ii], jj, sy.interact_same_bond_id)
     return float(np.sum(np.where(ok, st.pos_c.dtype.type(0.5) * e, 0).astype(np.float64)))
 
@@ -906,14 +962,18 @@ def compute_energy(st: OState, sy: OSystem, naive: bool = False):
     Returns ``(pe_pair, pe_gravity, ke_trans, ke_rot)``.
     """
     pe_pair = naive_energy(st, sy) if naive else cell_list_energy(st, sy, sum_dtype=np.float64)
+    # clump members carry the clump's mass and inertia: each counts 1 / count
+    # (thermal.py:24-80, force_manager.py:427-459)
+    count = np.bincount(st.clump_id, minlength=st.N)[st.clump_id].astype(np.float64)
+    w = st.mass.astype(np.float64) / count
     g = sy.gravity.astype(np.float64)
-    pe_grav = -float(np.sum((st.pos_c.astype(np.float64) @ g) * st.mass.astype(np.float64)))
-    ke_t = float(np.sum(0.5 * st.mass.astype(np.float64) * np.sum(st.vel.astype(np.float64) ** 2, axis=1)))
+    pe_grav = -float(np.sum((st.pos_c.astype(np.float64) @ g) * w))
+    ke_t = float(np.sum(0.5 * w * np.sum(st.vel.astype(np.float64) ** 2, axis=1)))
     if st.dim == 3:
         wb = quat_rotate_back(st.q, st.ang_vel).astype(np.float64)
     else:
         wb = st.ang_vel.astype(np.float64)
-    ke_r = float(np.sum(0.5 * np.sum(wb * (st.inertia.astype(np.float64) * wb), axis=1)))
+    ke_r = float(np.sum(0.5 * np.sum(wb * (st.inertia.astype(np.float64) * wb), axis=1) / count))
     return pe_pair, pe_grav, ke_t, ke_r
 
 
@@ -929,7 +989,7 @@ def contact_pairs(st: OState, sy: OSystem):
     stencil are considered, as in the reference.
     """
     N = st.N
-    pos = st.pos_c
+    pos = world_pos(st)
     cell = np.float32(2.0) * st.rad.max()
     sy2 = replace(sy)
     sy2.inv_box_size = sy.inv_box_size
@@ -945,6 +1005,7 @@ def contact_pairs(st: OState, sy: OSystem):
         hit = d_sq < R * R
         jj = np.arange(N)[None, :]
         hit &= jj > ii[:, None]
+        hit &= st.clump_id[ii][:, None] != st.clump_id[None, :]  # one clump: no contact
         bi, bj = np.nonzero(hit)
         out.append(np.stack([ii[bi], bj], 1))
     pairs = np.concatenate(out, 0) if out else np.zeros((0, 2), np.int64)

@@ -69,7 +69,7 @@ def test_config_struct_layout_matches_header(lib):
     from jaxdem_gb300._lib import Config, HostState, SystemDesc
 
     assert C.sizeof(SystemDesc) == 8 + 4 * 4 + 12 + 12 + 4 + 12 + 4 + 4
-    assert C.sizeof(HostState) == 12 * C.sizeof(C.c_void_p)
+    assert C.sizeof(HostState) == 14 * C.sizeof(C.c_void_p)
     assert C.sizeof(Config) >= 4 * 2 + C.sizeof(C.c_void_p)
 
 

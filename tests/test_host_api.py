@@ -93,8 +93,10 @@ def test_system_create_components_and_validation():
 def test_unsupported_configurations_raise_before_device_work():
     from jaxdem_gb300 import session
 
+    # rigid clumps are on the device path except in a reflect domain
     st = jdem.State.create(pos=np.zeros((4, 3)), clump_id=[0, 0, 1, 1])
-    sy = jdem.System.create(state=st, collider_type="CellList")
+    sy = jdem.System.create(state=st, collider_type="CellList", domain_type="reflect",
+                            domain_kw=dict(box_size=[5, 5, 5]))
     with pytest.raises(NotImplementedError):
         session.engine_for(st, sy)
     st2 = jdem.State.create(pos=np.zeros((4, 3)))

@@ -215,6 +215,63 @@ def test_cundall_strack_spin_slip_and_2d():
         assert np.allclose(f32, f, rtol=1e-5, atol=1e-6) and np.allclose(t32, t, rtol=1e-5, atol=1e-6)
 
 
+def test_rigid_clump_closed_forms():
+    """Rigid clumps (State.add_clump, state.py:1230-1420; ForceManager.apply,
+    force_manager.py:338-425): overlapping members of one clump exert nothing on each
+    other (colliders/__init__.py:225-243); contact forces between two clumps balance; a
+    contact at a member's offset r gives the clump the torque r x F about its centre;
+    gravity gives every member M g after the clump sum and no torque."""
+    f64 = np.float64
+    # two dumbbells along x: members at the centre +- (0.4, 0, 0), radius 0.5 (the members
+    # of one clump overlap by 0.2); clump B's left sphere overlaps clump A's right one
+    pc = np.array([[0.0, 0, 0], [0.0, 0, 0], [1.7, 0.3, 0], [1.7, 0.3, 0]])
+    pp = np.array([[-0.4, 0, 0], [0.4, 0, 0], [-0.4, 0, 0], [0.4, 0, 0]])
+    M, I = 2.0, [1.0, 1.0, 1.0]
+    st = R.make_state(pc, rad=[0.5] * 4, mass=[M] * 4, inertia=[I] * 4, pos_p=pp, clump_id=[0, 0, 1, 1],
+                      dtype=f64)
+    sy = _sys(3, domain="free", rad=st.rad, young=1e3, dtype=f64, gravity=[0, -9.8, 0])
+    f, t = R.cell_list_force(st, sy)
+    # only the A1-B0 pair touches across clumps: d = (1.7 - 0.4) - 0.4 = 0.9 along x, 0.3 along y
+    d = np.array([0.9, 0.3, 0.0])
+    r = np.linalg.norm(d)
+    fab = 1e3 * (1.0 - r) * d / r  # force on B0 from A1
+    assert np.allclose(f[0], 0) and np.allclose(f[3], 0)
+    assert np.allclose(f[2], fab, rtol=1e-12) and np.allclose(f[1], -fab, rtol=1e-12)
+    # torques about each clump centre: r x F with r = +-0.4 x
+    assert np.allclose(t[1], np.cross([0.4, 0, 0], -fab), rtol=1e-12)
+    assert np.allclose(t[2], np.cross([-0.4, 0, 0], fab), rtol=1e-12)
+    st.force, st.torque = f, t
+    st = R.force_manager_apply(st, sy)
+    g = np.array([0.0, -9.8, 0.0])
+    assert np.allclose(st.force[:2], -fab + M * g, rtol=1e-12) and np.allclose(st.force[2:], fab + M * g, rtol=1e-12)
+    assert np.allclose(st.torque[:2], np.cross([0.4, 0, 0], -fab)) and np.allclose(st.torque[2:], np.cross([-0.4, 0, 0], fab))
+    # the momentum exchanged balances
+    assert np.allclose(st.force[0] + st.force[2], 2 * M * g)
+    # contact set: the overlapping members of one clump are not contacts
+    assert R.contact_pairs(st, sy).tolist() == [[1, 2]]
+
+
+def test_rigid_clump_free_box_and_step():
+    """FreeDomain.apply with clumps (free.py:59-63) bounds pos_c -+ (|pos_p| + rad); a lone
+    spinning clump keeps its shape and centre velocity through the integrators."""
+    f64 = np.float64
+    pc = np.array([[1.0, 2.0, 3.0]] * 3)
+    pp = np.array([[0.3, 0, 0], [-0.3, 0, 0], [0, 0.6, 0]])
+    st = R.make_state(pc, rad=[0.2, 0.2, 0.3], mass=[3.0] * 3, inertia=[[0.5, 0.7, 0.9]] * 3, pos_p=pp,
+                      clump_id=[0, 0, 0], vel=[[0.1, 0.0, -0.2]] * 3, ang_vel=[[0.0, 0.0, 2.0]] * 3, dtype=f64)
+    sy = _sys(3, domain="free", rad=st.rad, dtype=f64, rotation="verletspiral")
+    R.free_apply(st, sy)
+    assert np.allclose(sy.anchor, np.array([1.0, 2.0, 3.0]) - 0.9) and np.allclose(sy.box_size, 1.8)
+    before = R.world_pos(st)
+    st, sy = R.step(st, sy, 50)
+    after = R.world_pos(st)
+    # rigid: pairwise distances of the members are unchanged, the centre drifts at v
+    dist = lambda p: np.linalg.norm(p[:, None] - p[None, :], axis=-1)
+    assert np.allclose(dist(after), dist(before), atol=1e-9)
+    assert np.allclose(st.pos_c[0], [1.0 + 50e-3 * 0.1, 2.0, 3.0 - 50e-3 * 0.2], atol=1e-12)
+    assert np.all(st.pos_c == st.pos_c[0]) and np.all(st.ang_vel == st.ang_vel[0])
+
+
 def test_periodic_image_pair():
     """Minimum image across the boundary (periodic.py:74-79)."""
     L = 10.0
