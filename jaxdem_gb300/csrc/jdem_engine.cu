@@ -269,6 +269,7 @@ int JdemHandle::ensure_capacity(long long p_need, int s_need) {
   b.rinertia = d_inertia;
   b.sys_of = st_sys;
   b.fixed_c = st_fixed;
+  b.rad_c = st_rad;
   return JDEM_OK;
 }
 

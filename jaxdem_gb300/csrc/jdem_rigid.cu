@@ -12,11 +12,11 @@
 //   k_rb_clump   per clump: ForceManager.apply -- F_contact + gravity * (M /
 //                count) summed over the members, torques summed
 //                (force_manager.py:338-425) -- then the integrators'
-//                after-force phase and, in MODE_STEP, the next step's free-domain
-//                box, before-force phase and drift;
+//                after-force phase and, in MODE_STEP, the next step's apply (free-domain
+//                box or reflect impulses), before-force phase and drift;
 //   k_rb_place   per slot: the member's new world position.
-// Members are summed in caller order.  Periodic and free domains; the
-// reflect domain's clump impulses (reflect.py:176-281) are not built.
+// Members are summed in caller order.  Periodic, free and reflect domains
+// (the reflect domain's clump impulses: clump_reflect).
 #include "jdem_device.cuh"
 #include "jdem_kernels.h"
 #include "jdem_pair.cuh"
@@ -102,10 +102,184 @@ __device__ __forceinline__ void load_clump(const Bufs& b, long long c, ClumpStat
   s.q = b.cq[c];
 }
 
+// ReflectDomain.apply for one rigid clump (domains/reflect.py:165-297): every
+// member's overshoot past the walls, the clump's deepest overshoot per axis;
+// the members holding it are active, each with the Verlet time-of-collision
+// fraction of its contact point (_toc.py:11-94), and the clump takes the
+// smallest; impulses -(1 + e) v_n / (1/m + (r x n) . I^-1 (r x n)), shared
+// among the active members of an axis, change the velocity and the angular
+// velocity (sums over the members in caller order), and the remaining part of
+// the step moves pos_c and q with the change.
+template <int DIM>
+__device__ void clump_reflect(const Bufs& b, const SysParams& sp, long long c, ClumpState& s) {
+  constexpr int AD = DIM == 3 ? 3 : 1;
+  const int m0 = b.cstart[c], m1 = b.cstart[c + 1];
+  const float dt = sp.dt, e = sp.restitution;
+  const float inv_mass = 1.0f / s.M;
+  // segment_max of the members' overshoots (all >= 0)
+  float max_lo[3] = {0, 0, 0}, max_hi[3] = {0, 0, 0};
+  for (int m = m0; m < m1; ++m) {
+    const long long i = b.cmember[m];
+    float r[3] = {0, 0, 0};
+    lever<DIM>(b, s.q, i, r);
+    const float rad = b.rad_c[i];
+    for (int a = 0; a < DIM; ++a) {
+      const float pos = s.p[a] + r[a];
+      const float lo = sp.anchor[a] + rad, hi = sp.anchor[a] + sp.box[a] - rad;
+      max_lo[a] = fmaxf(max_lo[a], fmaxf(0.0f, lo - pos));
+      max_hi[a] = fmaxf(max_hi[a], fmaxf(0.0f, pos - hi));
+    }
+  }
+  // angular acceleration of the clump: R (tau_b - w_b x (I w_b)) / I
+  float alpha_rot[3] = {0, 0, 0};
+  if (DIM == 3) {
+    float tb[3], wb[3], ab[3];
+    q_rotate3(s.q, -1.0f, s.T, tb);
+    q_rotate3(s.q, -1.0f, s.w, wb);
+    omega_dot3<3>(wb, tb, s.I, s.invI, ab);
+    q_rotate3(s.q, 1.0f, ab, alpha_rot);
+  } else {
+    alpha_rot[0] = s.T[0] * s.invI[0];
+  }
+  // body-frame wall normals n'_a = R^T e_a
+  float np_[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  const float4 qc = make_float4(s.q.x, -s.q.y, -s.q.z, -s.q.w);
+  for (int a = 0; a < DIM; ++a) {
+    float ea[3] = {0, 0, 0};
+    ea[a] = 1.0f;
+    if (DIM == 3) q_rotate3(s.q, -1.0f, ea, np_[a]);
+    else q_rotate2(qc, ea, np_[a]);
+  }
+  const float acc_c[3] = {s.F[0] * inv_mass, s.F[1] * inv_mass, DIM == 3 ? s.F[2] * inv_mass : 0.0f};
+  // pass 2: the clump's collision fraction and the active members per axis
+  float alpha_clump = 1.0f, count_active[3] = {0, 0, 0};
+  for (int m = m0; m < m1; ++m) {
+    const long long i = b.cmember[m];
+    float r[3] = {0, 0, 0};
+    lever<DIM>(b, s.q, i, r);
+    const float rad = b.rad_c[i];
+    float vcs[3], accc[3];
+    if (DIM == 3) {
+      vcs[0] = s.v[0] + (s.w[1] * r[2] - s.w[2] * r[1]);
+      vcs[1] = s.v[1] + (s.w[2] * r[0] - s.w[0] * r[2]);
+      vcs[2] = s.v[2] + (s.w[0] * r[1] - s.w[1] * r[0]);
+      accc[0] = acc_c[0] + (alpha_rot[1] * r[2] - alpha_rot[2] * r[1]);
+      accc[1] = acc_c[1] + (alpha_rot[2] * r[0] - alpha_rot[0] * r[2]);
+      accc[2] = acc_c[2] + (alpha_rot[0] * r[1] - alpha_rot[1] * r[0]);
+    } else {
+      vcs[0] = s.v[0] + -s.w[0] * r[1];
+      vcs[1] = s.v[1] + s.w[0] * r[0];
+      accc[0] = acc_c[0] + -alpha_rot[0] * r[1];
+      accc[1] = acc_c[1] + alpha_rot[0] * r[0];
+    }
+    float amin = 1.0f;
+    for (int a = 0; a < DIM; ++a) {
+      const float pos = s.p[a] + r[a];
+      const float lo = sp.anchor[a] + rad, hi = sp.anchor[a] + sp.box[a] - rad;
+      const float olo = fmaxf(0.0f, lo - pos), ohi = fmaxf(0.0f, pos - hi);
+      const float ws = ((olo > 0.0f && olo == max_lo[a]) ? 1.0f : 0.0f) - ((ohi > 0.0f && ohi == max_hi[a]) ? 1.0f : 0.0f);
+      const float act = fabsf(ws);
+      const float delta = fmaxf(max_lo[a], max_hi[a]);
+      const float al = toc_alpha(vcs[a], accc[a], delta, ws, dt);
+      amin = fminf(amin, act > 0.0f ? al : 1.0f);
+      count_active[a] = count_active[a] + act;
+    }
+    alpha_clump = fminf(alpha_clump, amin);
+  }
+  // pass 3: impulses
+  const float dt_factor = (alpha_clump - 1.0f) * dt;
+  float dv[3] = {0, 0, 0}, dw[3] = {0, 0, 0};
+  for (int m = m0; m < m1; ++m) {
+    const long long i = b.cmember[m];
+    float r[3] = {0, 0, 0};
+    lever<DIM>(b, s.q, i, r);
+    const float pp[3] = {b.spp[i * DIM], b.spp[i * DIM + 1], DIM == 3 ? b.spp[i * DIM + 2] : 0.0f};
+    const float rad = b.rad_c[i];
+    float vcs[3], accc[3];
+    if (DIM == 3) {
+      vcs[0] = s.v[0] + (s.w[1] * r[2] - s.w[2] * r[1]);
+      vcs[1] = s.v[1] + (s.w[2] * r[0] - s.w[0] * r[2]);
+      vcs[2] = s.v[2] + (s.w[0] * r[1] - s.w[1] * r[0]);
+      accc[0] = acc_c[0] + (alpha_rot[1] * r[2] - alpha_rot[2] * r[1]);
+      accc[1] = acc_c[1] + (alpha_rot[2] * r[0] - alpha_rot[0] * r[2]);
+      accc[2] = acc_c[2] + (alpha_rot[0] * r[1] - alpha_rot[1] * r[0]);
+    } else {
+      vcs[0] = s.v[0] + -s.w[0] * r[1];
+      vcs[1] = s.v[1] + s.w[0] * r[0];
+      accc[0] = acc_c[0] + -alpha_rot[0] * r[1];
+      accc[1] = acc_c[1] + alpha_rot[0] * r[0];
+    }
+    float J[3] = {0, 0, 0};
+    for (int a = 0; a < DIM; ++a) {
+      const float pos = s.p[a] + r[a];
+      const float lo = sp.anchor[a] + rad, hi = sp.anchor[a] + sp.box[a] - rad;
+      const float olo = fmaxf(0.0f, lo - pos), ohi = fmaxf(0.0f, pos - hi);
+      const float ws = ((olo > 0.0f && olo == max_lo[a]) ? 1.0f : 0.0f) - ((ohi > 0.0f && ohi == max_hi[a]) ? 1.0f : 0.0f);
+      const float act = fabsf(ws);
+      // denominator 1/m + sum_k invI_k (pos_p x n'_a)_k^2
+      float denom_rot;
+      if (DIM == 3) {
+        const float* n = np_[a];
+        const float cx = pp[1] * n[2] - pp[2] * n[1], cy = pp[2] * n[0] - pp[0] * n[2], cz = pp[0] * n[1] - pp[1] * n[0];
+        denom_rot = s.invI[0] * (cx * cx) + s.invI[1] * (cy * cy) + s.invI[2] * (cz * cz);
+      } else {
+        const float cz = pp[0] * np_[a][1] - pp[1] * np_[a][0];
+        denom_rot = s.invI[0] * (cz * cz);
+      }
+      float denom = inv_mass + denom_rot;
+      denom = denom == 0.0f ? 1.0f : denom;
+      const float vc = vcs[a] + dt_factor * accc[a];
+      float j = -(1.0f + e) * vc / denom;
+      const float closing = (vc * ws) < 0.0f ? 1.0f : 0.0f;
+      const float weight = act / fmaxf(count_active[a], 1.0f);
+      j = j * (weight * closing);
+      J[a] = j;
+      dv[a] = dv[a] + j * inv_mass;
+    }
+    // angular: moment of the impulse about the centre in the body frame
+    if (DIM == 3) {
+      float jb[3], mb[3], dl[3];
+      q_rotate3(s.q, -1.0f, J, jb);
+      mb[0] = (pp[1] * jb[2] - pp[2] * jb[1]) * s.invI[0];
+      mb[1] = (pp[2] * jb[0] - pp[0] * jb[2]) * s.invI[1];
+      mb[2] = (pp[0] * jb[1] - pp[1] * jb[0]) * s.invI[2];
+      q_rotate3(s.q, 1.0f, mb, dl);
+      for (int a = 0; a < 3; ++a) dw[a] = dw[a] + dl[a];
+    } else {
+      float jb[2];
+      q_rotate2(qc, J, jb);
+      dw[0] = dw[0] + (pp[0] * jb[1] - pp[1] * jb[0]) * s.invI[0];
+    }
+  }
+  const bool fixed = s.fr == 0.0f;
+  const float dt_rem = (1.0f - alpha_clump) * dt;
+  for (int a = 0; a < DIM; ++a) {
+    const float d = fixed ? 0.0f : dv[a];
+    s.v[a] = s.v[a] + d;
+    dv[a] = d;
+  }
+  for (int a = 0; a < AD; ++a) {
+    dw[a] = fixed ? 0.0f : dw[a];
+    s.w[a] = s.w[a] + dw[a];
+  }
+  float th[3];
+  if (DIM == 3) {
+    for (int a = 0; a < 3; ++a) th[a] = dw[a] * dt_rem;
+  } else {
+    th[0] = 0.0f;
+    th[1] = 0.0f;
+    th[2] = dw[0] * dt_rem;
+  }
+  s.q = q_unit(q_mul(q_small_rotvec(th[0], th[1], th[2]), s.q));
+  for (int a = 0; a < DIM; ++a) s.p[a] = s.p[a] + dv[a] * dt_rem;
+}
+
 // The next step's apply (free domain: the box of pos_c -+ (|pos_p| + rad),
-// free.py:59-63), then step_before_force of both integrators and the drift.
+// free.py:59-63; reflect: clump_reflect), then step_before_force of both
+// integrators and the drift.
 template <int DIM>
 __device__ __forceinline__ void clump_before(const Bufs& b, const SysParams& sp, long long c, int mode, ClumpState& s) {
+  if (sp.domain == DOM_REFLECT) clump_reflect<DIM>(b, sp, c, s);
   if ((mode & MODE_BBOX) && sp.domain == DOM_FREE) {
     const int sys = b.csys[c];
     const float br = b.cbrad[c];
@@ -469,9 +643,6 @@ int JdemHandle::setup_clumps(const JdemHostState* s, bool device_ptrs) {
   }
   const long long NC = (long long)count.size();
   if (NC == (long long)N && !offset) return JDEM_OK;  // spheres
-  for (int s2 = 0; s2 < S; ++s2)
-    if (desc[s2].domain == DOM_REFLECT)
-      return fail(JDEM_ERR_UNSUPPORTED, "rigid clumps in a reflect domain are not supported");
   if (b.law == LAW_CS) return fail(JDEM_ERR_UNSUPPORTED, "rigid clumps with Cundall-Strack contacts are not supported");
   std::vector<int32_t> start((size_t)NC + 1, 0), member(N);
   for (long long c = 0; c < NC; ++c) start[(size_t)c + 1] = start[(size_t)c] + count[(size_t)c];

@@ -8,7 +8,7 @@ captured CUDA graphs; each call uploads the caller's state, runs, and reads
 the result back (the functional contract of the reference API).
 
 Configurations outside the GB300 hot path raise ``NotImplementedError``:
-rigid clumps in a reflect domain or with Cundall-Strack contacts, facets, bonded force models,
+rigid clumps with Cundall-Strack contacts, facets, bonded force models,
 force models other than ``spring``, ``hertz`` and ``cundallstrack``, user force functions, pending external
 forces and user pre/post-step actions.
 """
@@ -61,8 +61,6 @@ def _check_supported(state: State, system) -> None:
     if system.user_pre_step_actions is not _save_state_system or system.user_post_step_actions is not _save_state_system:
         raise NotImplementedError("user pre/post step actions are outside the GB300 hot path")
     if _has_clumps(state):
-        if system.domain.type_name == "reflect":
-            raise NotImplementedError("rigid clumps in a reflect domain are not supported by the GB300 engine")
         if system.force_model.type_name == "cundallstrack":
             raise NotImplementedError("rigid clumps with Cundall-Strack contacts are not supported by the GB300 engine")
     if state.facet_id.size and np.any(state.facet_id != -1):

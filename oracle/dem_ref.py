@@ -656,7 +656,7 @@ def reflect_apply(st: OState, sy: OSystem):
     ``count_active`` equals ``active``.
     """
     if st.rigid:
-        raise NotImplementedError("the oracle's reflect domain is restated for spheres only")
+        return reflect_apply_clumps(st, sy)
     t = st.pos_c.dtype.type
     e = t(sy.restitution)
     pos = st.pos_c
@@ -688,6 +688,104 @@ def reflect_apply(st: OState, sy: OSystem):
     dt_rem = (t(1) - alpha_min) * sy.dt
     # q <- unit(dq @ q) with dq = from_small_rotvec(0) = (1, 0): reflect.py:291-294
     st.q = quat_unit(quat_mul(np.concatenate([np.ones_like(st.q[:, :1]), np.zeros_like(st.q[:, 1:])], 1), st.q))
+    st.pos_c = st.pos_c + dv * dt_rem
+    return st
+
+
+def _segment(values, ids, n, op):
+    """``jax.ops.segment_{sum,max,min}`` over the leading axis, in index order."""
+    if op == "sum":
+        out = np.zeros((n,) + values.shape[1:], values.dtype)
+        for i in range(values.shape[0]):
+            out[ids[i]] = out[ids[i]] + values[i]
+        return out
+    init = -np.inf if op == "max" else np.inf
+    out = np.full((n,) + values.shape[1:], init, values.dtype)
+    f = np.maximum if op == "max" else np.minimum
+    for i in range(values.shape[0]):
+        out[ids[i]] = f(out[ids[i]], values[i])
+    return out
+
+
+def reflect_apply_clumps(st: OState, sy: OSystem):
+    """``ReflectDomain.apply`` (``domains/reflect.py:99-299``) for rigid clumps: the
+    clump's deepest overshoot per axis, the Verlet collision fraction of each active
+    member's contact point and the clump minimum, impulses shared by the active members,
+    linear and angular velocity changes summed over the clump, then the position and
+    orientation corrections over the rest of the step."""
+    t = st.pos_c.dtype.type
+    N, d = st.N, st.dim
+    cid = st.clump_id
+    e = t(sy.restitution)
+    dt = sy.dt
+    pos_p_lab = pos_p_rot(st)
+    pos = st.pos_c + pos_p_lab
+    rad = st.rad[:, None]
+    lo = sy.anchor + rad
+    hi = sy.anchor + sy.box_size - rad
+    over_lo = np.maximum(t(0), lo - pos)
+    over_hi = np.maximum(t(0), pos - hi)
+    max_lo = _segment(over_lo, cid, N, "max")[cid]
+    max_hi = _segment(over_hi, cid, N, "max")[cid]
+    inv_mass = t(1.0) / st.mass
+    inv_inertia = t(1.0) / st.inertia
+    eye = np.eye(d, dtype=st.pos_c.dtype)
+    # n_prime[:, a, :] = rotate_back(q, e_a): the rows of the rotation matrix
+    n_prime = np.stack([quat_rotate_back(st.q, np.broadcast_to(eye[a], (N, d)).copy()) for a in range(d)], 1)
+    if d == 3:
+        rpcn = np.stack([cross3(st.pos_p, n_prime[:, a, :]) for a in range(3)], 1)
+    else:
+        rpcn = np.stack([st.pos_p[:, 0:1] * n_prime[:, a, 1:2] - st.pos_p[:, 1:2] * n_prime[:, a, 0:1]
+                         for a in range(2)], 1)
+    denom_rot = np.einsum("ni,nji->nj", inv_inertia, rpcn * rpcn).astype(st.pos_c.dtype)
+    denom = inv_mass[:, None] + denom_rot
+    denom = np.where(denom == 0, t(1), denom)
+    delta = np.maximum(max_lo, max_hi)
+    deep_lo = (over_lo > 0) & (over_lo == max_lo)
+    deep_hi = (over_hi > 0) & (over_hi == max_hi)
+    wall_sign = deep_lo.astype(st.pos_c.dtype) - deep_hi.astype(st.pos_c.dtype)
+    active = np.abs(wall_sign)
+    v_contact_step = st.vel + _cross_w(st.ang_vel, pos_p_lab)
+    acc_clump = st.force * inv_mass[:, None]
+    if d == 3:
+        Rm = n_prime
+        RT = np.swapaxes(n_prime, -1, -2)
+        tb = np.einsum("nij,nj->ni", RT, st.torque).astype(st.pos_c.dtype)
+        wb = np.einsum("nij,nj->ni", RT, st.ang_vel).astype(st.pos_c.dtype)
+        ab = (tb - cross3(wb, st.inertia * wb)) * inv_inertia
+        alpha_rot = np.einsum("nij,nj->ni", Rm, ab).astype(st.pos_c.dtype)
+    else:
+        alpha_rot = st.torque * inv_inertia
+    acc_contact = acc_clump + _cross_w(alpha_rot, pos_p_lab)
+    alpha = verlet_collision_fraction(v_contact_step, acc_contact, delta, wall_sign, dt)
+    alpha_min_dim = np.min(np.where(active > 0, alpha, t(1)), axis=-1, keepdims=True)
+    alpha_clump = _segment(alpha_min_dim, cid, N, "min")[cid]
+    dt_factor = (alpha_clump - t(1)) * dt
+    v_contact = v_contact_step + dt_factor * acc_contact
+    j = -(t(1) + e) * v_contact / denom
+    closing = (v_contact * wall_sign) < 0
+    count_active = _segment(active, cid, N, "sum")
+    weight = active / np.maximum(count_active, t(1))[cid]
+    j = j * (weight * closing.astype(st.pos_c.dtype))
+    dv = _segment(j * inv_mass[:, None], cid, N, "sum")[cid]
+    dv = np.where(st.fixed[:, None], t(0), dv)
+    st.vel = st.vel + dv
+    if d == 3:
+        jb = np.einsum("nij,nj->ni", RT, j).astype(st.pos_c.dtype)
+        mom = cross3(st.pos_p, jb)
+        dwl = np.einsum("nij,nj->ni", Rm, mom * inv_inertia).astype(st.pos_c.dtype)
+    else:
+        jb = np.einsum("nji,nj->ni", n_prime, j).astype(st.pos_c.dtype)
+        mom = st.pos_p[:, 0:1] * jb[:, 1:2] - st.pos_p[:, 1:2] * jb[:, 0:1]
+        dwl = mom * inv_inertia
+    dw = _segment(dwl, cid, N, "sum")[cid]
+    dw = np.where(st.fixed[:, None], t(0), dw)
+    st.ang_vel = st.ang_vel + dw
+    dt_rem = (t(1) - alpha_clump) * dt
+    theta = dw * dt_rem
+    if d == 2:
+        theta = np.concatenate([np.zeros_like(theta), np.zeros_like(theta), theta], axis=-1)
+    st.q = quat_unit(quat_mul(quat_from_small_rotvec(theta), st.q))
     st.pos_c = st.pos_c + dv * dt_rem
     return st
 

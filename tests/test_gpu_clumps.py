@@ -152,9 +152,43 @@ def test_clump_rollout_matches_oracle(dim, domain, linear, gravity, steps=50):
         assert np.allclose(anc[0], sy.anchor, rtol=1e-5, atol=1e-5)
 
 
-def test_clump_reflect_is_refused():
+@pytest.mark.parametrize("dim", [3, 2])
+def test_clump_reflect_rollout_matches_oracle(dim, steps=200):
+    """Clumps falling onto the floor of a reflect box (reflect.py:165-297): wall impulses
+    with spin, the clump's collision fraction and the remaining-step corrections."""
+    c = clump_system(n_clumps=300, dim=dim, seed=85 + dim, phi=0.25)
+    # every member inside the box at the start (|pos_p| + rad <= 0.85)
+    c["pos_c"] = (1.0 + c["pos_c"] * (c["L"] - 2.0) / c["L"]).astype(F32)
+    g = np.zeros(dim, F32)
+    g[1] = -20.0
+    st, sy = ostate_sys(c, domain="reflect", gravity=g)
+    sy.restitution = F32(0.7)
+    st, sy = R.step(st, sy, steps, sum_dtype=np.float64)
+    desc = dict(n=c["N"], domain="reflect", linear="verlet", rotation="verletspiral", dt=1e-3,
+                box_size=np.full(dim, c["L"], F32), anchor=np.zeros(dim, F32), restitution=0.7, gravity=g,
+                cell_size=1.0, search_range=1)
+    eng = Engine(dim, [desc], K, skin=0.1)
+    try:
+        upload(eng, c)
+        eng.step(steps)
+        out = eng.download()
+    finally:
+        eng.close()
+    assert min_image_diff(out["pos_c"], st.pos_c) <= 1e-4
+    assert np.abs(out["vel"] - st.vel).max() <= 1e-3 * max(1.0, np.abs(st.vel).max())
+    assert np.abs(out["ang_vel"] - st.ang_vel).max() <= 1e-3 * max(1.0, np.abs(st.ang_vel).max())
+    assert np.abs(out["q"] - st.q).max() <= 1e-4
+    # clumps hit the floor and bounced
+    assert np.any(st.vel[:, 1] > 0.5)
+
+
+def test_clumps_with_cundall_strack_are_refused():
     c = clump_system(n_clumps=50, seed=80)
-    eng = engine(c, domain="reflect")
+    beta, props = R.cs_tables([1e3], [0.3], [0.5], [0.3], [0.0])
+    desc = dict(n=c["N"], domain="periodic", linear="verlet", rotation="verletspiral", dt=1e-3,
+                box_size=np.full(3, c["L"], F32), anchor=np.zeros(3, F32), restitution=1.0,
+                gravity=np.zeros(3, F32), cell_size=1.0, search_range=1)
+    eng = Engine(3, [desc], beta, skin=0.1, force_law="cundallstrack", material_props=props)
     try:
         with pytest.raises(JdemError):
             upload(eng, c)

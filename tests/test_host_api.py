@@ -93,10 +93,11 @@ def test_system_create_components_and_validation():
 def test_unsupported_configurations_raise_before_device_work():
     from jaxdem_gb300 import session
 
-    # rigid clumps are on the device path except in a reflect domain
-    st = jdem.State.create(pos=np.zeros((4, 3)), clump_id=[0, 0, 1, 1])
-    sy = jdem.System.create(state=st, collider_type="CellList", domain_type="reflect",
-                            domain_kw=dict(box_size=[5, 5, 5]))
+    # rigid clumps are on the device path except with Cundall-Strack contacts
+    mats = [jdem.Material.create("elasticfrict", young=1e3, poisson=0.3, e=0.5, mu=0.3)]
+    table = jdem.MaterialTable.from_materials(mats)
+    st = jdem.State.create(pos=np.zeros((4, 3)), clump_id=[0, 0, 1, 1], mat_table=table)
+    sy = jdem.System.create(state=st, collider_type="CellList", mat_table=table, force_model_type="cundallstrack")
     with pytest.raises(NotImplementedError):
         session.engine_for(st, sy)
     st2 = jdem.State.create(pos=np.zeros((4, 3)))

@@ -272,6 +272,33 @@ def test_rigid_clump_free_box_and_step():
     assert np.all(st.pos_c == st.pos_c[0]) and np.all(st.ang_vel == st.ang_vel[0])
 
 
+def test_rigid_clump_wall_impulse_closed_form():
+    """ReflectDomain.apply for a clump (reflect.py:165-297): a tilted dumbbell whose lower
+    member crosses the wall y = 0 with no force acting (acc = 0, so the contact velocity is
+    the end-of-step one): with e = 1 the impulse -(1 + e) v_n / (1/m + (r x n) . I^-1 (r x n))
+    reverses the contact point's normal velocity and keeps the kinetic energy (translation
+    plus rotation); the clump starts to spin."""
+    f64 = np.float64
+    th = np.pi / 6
+    q = np.array([np.cos(th / 2), 0, 0, np.sin(th / 2)])  # 30 degrees about z
+    pp = np.array([[-0.4, 0, 0], [0.4, 0, 0]])
+    M, I = 2.0, np.array([0.3, 0.5, 0.6])
+    st = R.make_state(np.array([[3.0, 0.49, 3.0]] * 2), rad=[0.3, 0.3], mass=[M] * 2, inertia=[I] * 2,
+                      pos_p=pp, clump_id=[0, 0], vel=[[0.2, -1.0, 0.0]] * 2, q=[q] * 2, dtype=f64)
+    sy = _sys(3, domain="reflect", box=[10, 10, 10], rad=st.rad, dtype=f64)
+    sy.restitution = f64(1.0)
+    r = R.pos_p_rot(st)
+    ke = lambda s: 0.5 * M * s.vel[0] @ s.vel[0] + 0.5 * (R.quat_rotate_back(s.q, s.ang_vel)[0] ** 2 @ I)
+    vc_before = st.vel[0] + np.cross(st.ang_vel[0], r[0])
+    e0 = ke(st)
+    st2 = R.reflect_apply(st.copy(), sy)
+    assert np.isclose(ke(st2), e0, rtol=1e-12)
+    # the lower member (index 0, at -0.4 rotated: y = 0.49 - 0.2) took the impulse
+    vc_now = st2.vel[0] + np.cross(st2.ang_vel[0], r[0])
+    assert np.isclose(vc_now[1], -vc_before[1], rtol=1e-12)
+    assert abs(st2.ang_vel[0, 2]) > 0.1 and np.array_equal(st2.ang_vel[0], st2.ang_vel[1])
+
+
 def test_periodic_image_pair():
     """Minimum image across the boundary (periodic.py:74-79)."""
     L = 10.0
