@@ -304,9 +304,9 @@ def run_ours(args, rank, world, dist):
         cpu = cpu_baseline(w, args.cpu_seconds)
 
     value = replicas.aggregate_throughput([w.N * K] * world, total_ms * 1e-3)
-    # per call: k_pre; per step: k_cond + k_force; per re-sort: 7 sort kernels + the list build
+    # per chunk: k_cond; per step: k_force + k_fin; per re-sort: 8 sort kernels + the list build
     rebuilds_timed = stats["rebuilds"] - rebuilds_before
-    launches = sum(1 + 2 * c for c in chunks) + 8 * rebuilds_timed
+    launches = sum(1 + 2 * c for c in chunks) + 9 * rebuilds_timed
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,

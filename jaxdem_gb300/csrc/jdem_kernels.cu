@@ -191,7 +191,16 @@ __global__ void k_bin(Bufs b) {
   }
   int key = (int)(sp.c0 + local);
   b.key_tmp[t] = key;
-  b.slot_tmp[t] = atomicAdd(&b.cnt[key], 1);
+  // one atomic per distinct cell of the warp: slots are ordered by cell since
+  // the last re-sort, so neighbouring lanes mostly share a cell
+  const unsigned int active = __activemask();
+  const unsigned int peers = __match_any_sync(active, key);
+  const int leader = __ffs(peers) - 1;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&b.cnt[key], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  b.slot_tmp[t] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_TILE = SCAN_T * SCAN_V;
@@ -309,10 +318,10 @@ __global__ void k_cellsort(Bufs b) {
   }
 }
 
-// Gather every slot array into the spare copy in sorted order, then flip.
+// Gather every slot array into the spare copy in sorted order (k_sort_fin
+// then flips the copies).
 __global__ void k_gather(Bufs b) {
   if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
-  __shared__ bool is_last;
   long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   if (u < b.P) {
@@ -348,23 +357,17 @@ __global__ void k_gather(Bufs b) {
     b.orig[sel ^ 1u][u] = b.orig[sel][t];
     b.key[sel ^ 1u][u] = b.key_tmp[t];
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    unsigned int prev = atomicAdd(&b.ctl->done2, 1u);
-    is_last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (is_last && threadIdx.x == 0) {
-    __threadfence();
-    b.ctl->sel = sel ^ 1u;
-    b.ctl->pos_sel = ps ^ 1u;
-    b.ctl->need_rebuild = 0u;
-    b.ctl->nl_dirty = 1u;
-    b.ctl->bound = 0.0f;
-    b.ctl->rebuilds += 1u;
-    b.ctl->done2 = 0u;
-  }
+}
+
+// After k_gather: the sorted copies become current and the list is due.
+__global__ void k_sort_fin(Ctl* ctl) {
+  if (ctl->need_rebuild == 0u) return;
+  ctl->sel ^= 1u;
+  ctl->pos_sel ^= 1u;
+  ctl->need_rebuild = 0u;
+  ctl->nl_dirty = 1u;
+  ctl->bound = 0.0f;
+  ctl->rebuilds += 1u;
 }
 
 // ------------------------------------------------------------ first drift
@@ -952,9 +955,10 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st) {
   k_scatter<<<nblk(b.P, 256), 256, 0, st>>>(b);
   k_cellsort<<<nblk(b.C, 256), 256, 0, st>>>(b);
   k_gather<<<nblk(b.P, 256), 256, 0, st>>>(b);
+  k_sort_fin<<<1, 1, 0, st>>>(b.ctl);
 }
 
-int rebuild_kernel_count(bool any_free) { return any_free ? 8 : 7; }
+int rebuild_kernel_count(bool any_free) { return any_free ? 9 : 8; }
 
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
