@@ -1079,7 +1079,7 @@ int jdem_create(const JdemConfig* cfg, JdemHandle** out) {
   *out = nullptr;
   JdemHandle* h = new (std::nothrow) JdemHandle();
   if (!h) return JDEM_ERR_OOM;
-  int rc = h->setup(cfg);
+  int rc = jdem_guard(&h->err, [&] { return h->setup(cfg); });
   if (rc) {
     std::fprintf(stderr, "jdem_create: %s\n", h->err.c_str());
     h->free_all();
@@ -1101,59 +1101,72 @@ int jdem_destroy(JdemHandle* h) {
 
 const char* jdem_last_error(const JdemHandle* h) { return h ? h->err.c_str() : "null handle"; }
 
-int jdem_upload(JdemHandle* h, const JdemHostState* s) { return h ? h->upload(s, false) : JDEM_ERR_BAD_ARG; }
-int jdem_upload_device(JdemHandle* h, const JdemHostState* s) { return h ? h->upload(s, true) : JDEM_ERR_BAD_ARG; }
+int jdem_upload(JdemHandle* h, const JdemHostState* s) {
+  return h ? jdem_guard(&h->err, [&] { return h->upload(s, false); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_upload_device(JdemHandle* h, const JdemHostState* s) {
+  return h ? jdem_guard(&h->err, [&] { return h->upload(s, true); }) : JDEM_ERR_BAD_ARG;
+}
 
 int jdem_step(JdemHandle* h, int64_t n) {
   if (!h) return JDEM_ERR_BAD_ARG;
-  int rc = h->step_async(n);
-  if (rc) return rc;
-  return h->sync_status();
+  return jdem_guard(&h->err, [&] {
+    int rc = h->step_async(n);
+    return rc ? rc : h->sync_status();
+  });
 }
 
-int jdem_step_async(JdemHandle* h, int64_t n) { return h ? h->step_async(n) : JDEM_ERR_BAD_ARG; }
-int jdem_sync(JdemHandle* h) { return h ? h->sync_status() : JDEM_ERR_BAD_ARG; }
+int jdem_step_async(JdemHandle* h, int64_t n) {
+  return h ? jdem_guard(&h->err, [&] { return h->step_async(n); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_sync(JdemHandle* h) { return h ? jdem_guard(&h->err, [&] { return h->sync_status(); }) : JDEM_ERR_BAD_ARG; }
 
 int jdem_step_timed(JdemHandle* h, int64_t n, double* total_ms, double* force_ms) {
-  return h ? h->step_timed(n, total_ms, force_ms) : JDEM_ERR_BAD_ARG;
+  return h ? jdem_guard(&h->err, [&] { return h->step_timed(n, total_ms, force_ms); }) : JDEM_ERR_BAD_ARG;
 }
 
-int jdem_download(JdemHandle* h, JdemHostState* s) { return h ? h->download(s, false) : JDEM_ERR_BAD_ARG; }
-int jdem_download_device(JdemHandle* h, JdemHostState* s) { return h ? h->download(s, true) : JDEM_ERR_BAD_ARG; }
-int jdem_compute_force(JdemHandle* h) { return h ? h->compute_force() : JDEM_ERR_BAD_ARG; }
+int jdem_download(JdemHandle* h, JdemHostState* s) {
+  return h ? jdem_guard(&h->err, [&] { return h->download(s, false); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_download_device(JdemHandle* h, JdemHostState* s) {
+  return h ? jdem_guard(&h->err, [&] { return h->download(s, true); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_compute_force(JdemHandle* h) {
+  return h ? jdem_guard(&h->err, [&] { return h->compute_force(); }) : JDEM_ERR_BAD_ARG;
+}
 
 int jdem_energy(JdemHandle* h, double out[4]) {
   if (!h || !out) return JDEM_ERR_BAD_ARG;
-  return h->energy(out, false);
+  return jdem_guard(&h->err, [&] { return h->energy(out, false); });
 }
 
 int jdem_energy_per_system(JdemHandle* h, double* out) {
   if (!h || !out) return JDEM_ERR_BAD_ARG;
-  return h->energy(out, true);
+  return jdem_guard(&h->err, [&] { return h->energy(out, true); });
 }
 
 int jdem_contacts(JdemHandle* h, int32_t* pairs, int64_t cap, int64_t* count) {
   if (!h) return JDEM_ERR_BAD_ARG;
   long long c = 0;
-  int rc = h->contacts(pairs, cap, &c);
+  int rc = jdem_guard(&h->err, [&] { return h->contacts(pairs, cap, &c); });
   if (count) *count = c;
   return rc;
 }
 
 int jdem_neighbor_list(JdemHandle* h, float cutoff, int32_t max_neighbors, int32_t* out, int32_t* overflow) {
   if (!h) return JDEM_ERR_BAD_ARG;
-  return h->neighbor_list(cutoff, max_neighbors, out, overflow);
+  return jdem_guard(&h->err, [&] { return h->neighbor_list(cutoff, max_neighbors, out, overflow); });
 }
 
 int jdem_domain_state(JdemHandle* h, float* box, float* anchor) {
   if (!h) return JDEM_ERR_BAD_ARG;
-  return h->domain_state(box, anchor);
+  return jdem_guard(&h->err, [&] { return h->domain_state(box, anchor); });
 }
 
 int jdem_stats(JdemHandle* h, JdemStats* out) {
   if (!h || !out) return JDEM_ERR_BAD_ARG;
   if (h->uploaded) {
-    int rc = h->sync_status();
+    int rc = jdem_guard(&h->err, [&] { return h->sync_status(); });
     if (rc && rc != JDEM_ERR_NONFINITE) return rc;
   }
   out->n_particles = h->P;

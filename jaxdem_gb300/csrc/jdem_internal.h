@@ -1,6 +1,7 @@
 // Host-side handle of the GB300 DEM step engine (not part of the public ABI).
 #pragma once
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,30 @@
                        std::string(#expr) + ": " + cudaGetErrorString(_e));            \
     }                                                                                   \
   } while (0)
+
+struct JdemHandle;
+
+// Runs the body of an entry point: a C++ exception (a failed host allocation,
+// thread creation) becomes an error status and never crosses the C boundary.
+template <typename F>
+int jdem_guard(std::string* err, F&& body) noexcept {
+  const char* what = "internal error";
+  int code = JDEM_ERR_CUDA;
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    what = "host allocation failed";
+    code = JDEM_ERR_OOM;
+  } catch (...) {
+  }
+  if (err) {
+    try {
+      *err = what;
+    } catch (...) {
+    }
+  }
+  return code;
+}
 
 struct JdemHandle {
   // configuration

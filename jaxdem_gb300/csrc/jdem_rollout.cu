@@ -75,7 +75,15 @@ class Prefault {
     page_ = ps > 0 ? (size_t)ps : 4096;
     unsigned hw = std::thread::hardware_concurrency();
     int n = (int)std::min<long long>(T, std::max(1u, std::min(8u, hw / 2)));
-    for (int w = 0; w < n; ++w) workers_.emplace_back([this, w, n] { run(w, n); });
+    try {
+      for (int w = 0; w < n; ++w) workers_.emplace_back([this, w, n] { run(w, n); });
+    } catch (...) {
+      // no threads: stop the ones started and copy without the pre-touch
+      stop_.store(true);
+      for (auto& th : workers_) th.join();
+      workers_.clear();
+      for (long long t = 0; t < T; ++t) done_[t].store(1, std::memory_order_relaxed);
+    }
   }
   ~Prefault() {
     stop_.store(true);
@@ -286,5 +294,5 @@ int JdemHandle::rollout(const int64_t* strides, long long T, const JdemFrames* o
 
 extern "C" int jdem_rollout(JdemHandle* h, const int64_t* strides, int64_t n_frames, const JdemFrames* out) {
   if (!h) return JDEM_ERR_BAD_ARG;
-  return h->rollout(strides, (long long)n_frames, out);
+  return jdem_guard(&h->err, [&] { return h->rollout(strides, (long long)n_frames, out); });
 }

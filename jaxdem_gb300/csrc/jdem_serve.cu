@@ -83,6 +83,7 @@ struct JdemServer {
   std::vector<Req*> graveyard;
   std::thread worker;
   bool stop = false;
+  bool broken = false;  // the worker stopped on a host error: requests fail
   int64_t next_id = 1;
   Staging st[2];
   int cur = 0;            // staging holding the live batch layout
@@ -105,6 +106,7 @@ struct JdemServer {
   int repack(std::vector<Req*>& next);
   int finish(std::vector<Req*>& done);
   void loop();
+  void run_epochs();
   void reap();
 };
 
@@ -269,7 +271,38 @@ void JdemServer::reap() {
   graveyard.resize(k);
 }
 
+// The worker thread.  A C++ exception (a failed host allocation) ends the
+// loop: every pending and live request fails with JDEM_ERR_OOM, waiters are
+// woken, and later submissions are refused.
 void JdemServer::loop() {
+  try {
+    run_epochs();
+  } catch (...) {
+    std::lock_guard<std::mutex> lk(mtx);
+    broken = true;
+    err = "serve: host allocation failed in the worker";
+    double t = now_s();
+    for (auto& kv : all) {
+      Req* r = kv.second;
+      if (r->state != REQ_PENDING && r->state != REQ_ACTIVE) continue;
+      if (r->state == REQ_ACTIVE) {
+        bytes_in_use -= r->bytes;
+        n_active -= 1;
+      }
+      r->state = REQ_FAILED;
+      r->status = JDEM_ERR_OOM;
+      r->t_done = t;
+      unfinished -= 1;
+      finished_unpolled.push_back(r->id);
+    }
+    pending.clear();
+    active.clear();
+    stats.failures += 1;
+    done_cv.notify_all();
+  }
+}
+
+void JdemServer::run_epochs() {
   cudaSetDevice(cfg.device);
   for (;;) {
     std::vector<Req*> next, done, dropped;
@@ -426,7 +459,13 @@ int jdem_serve_create(const JdemServeConfig* cfg, JdemServer** out) {
     delete s;
     return rc;
   }
-  s->worker = std::thread([s] { s->loop(); });
+  try {
+    s->worker = std::thread([s] { s->loop(); });
+  } catch (...) {
+    jdem_destroy(s->h);
+    delete s;
+    return JDEM_ERR_OOM;
+  }
   *out = s;
   return JDEM_OK;
 }
@@ -475,6 +514,7 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
       cudaMallocHost((void**)&r->o_pos, vec) != cudaSuccess || cudaMallocHost((void**)&r->o_vel, vec) != cudaSuccess ||
       cudaMallocHost((void**)&r->o_frc, vec) != cudaSuccess) {
     cudaGetLastError();
+    free_req(r);
     return JDEM_ERR_OOM;
   }
   std::memcpy(r->h_pos, req->pos, 4 * n * d);
@@ -490,9 +530,19 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
   }
   {
     std::lock_guard<std::mutex> lk(s->mtx);
+    if (s->broken) {
+      free_req(r);
+      return JDEM_ERR_CUDA;
+    }
     r->id = s->next_id++;
-    s->all[r->id] = r;
-    s->pending.push_back(r);
+    try {
+      s->all[r->id] = r;
+      s->pending.push_back(r);
+    } catch (...) {
+      s->all.erase(r->id);
+      free_req(r);
+      return JDEM_ERR_OOM;
+    }
     s->unfinished += 1;
     s->stats.submitted += 1;
   }
@@ -551,8 +601,12 @@ int jdem_serve_release(JdemServer* s, int64_t id) {
   if (it == s->all.end()) return JDEM_ERR_BAD_ARG;
   Req* r = it->second;
   if (r->state == REQ_PENDING || r->state == REQ_ACTIVE) return JDEM_ERR_NOT_READY;
+  try {
+    s->graveyard.push_back(r);
+  } catch (...) {
+    return JDEM_ERR_OOM;  // still registered: release can be retried
+  }
   s->all.erase(it);
-  s->graveyard.push_back(r);
   s->cv.notify_one();
   return JDEM_OK;
 }
