@@ -158,6 +158,7 @@ __global__ void k_cs_force(Bufs b) {
   if (use_list) {
     const int n = b.ncnt[t];
     const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
+    prefetch_list_block(b, t, n);
     for (int k = 0; k < n; ++k) {
       const uint32_t e = (uint32_t)nb[k * 32];
       visit((int)(e & kEntrySlot), (e & kEntryImage) != 0u);

@@ -536,6 +536,11 @@ __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
   if (t < b.P) {
     const int n = use_list ? b.ncnt[t] : 0;
     const int32_t* nb = use_list ? b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31) : nullptr;
+    if (use_list) {
+      prefetch_list_block(b, t, n);
+      // the velocity record, read after the contact loop
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(&b.vel[sel][t]));
+    }
     d2max = particle_step<DIM, GENERAL, LAW>(b, mode, t, sel, ps, use_list, nb, n, 32);
   }
   if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);

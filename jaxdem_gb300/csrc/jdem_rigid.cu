@@ -53,6 +53,7 @@ __global__ void k_rb_force(Bufs b) {
   if (use_list) {
     const int n = b.ncnt[t];
     const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
+    prefetch_list_block(b, t, n);
     for (int k = 0; k < n; ++k) {
       const uint32_t e = (uint32_t)nb[k * 32];
       acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], true);
