@@ -305,26 +305,28 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
       for (int dy = -1; dy <= 1; ++dy) {
         const int vb = ((iz + dz) * bk.VY + (iy + dy)) * bk.VX + ix - 1;
         const int oa = vstart[vb], ob = vstart[vb + 3];
-        for (int o = oa; o < ob; o += 4) {
+        auto test = [&](int oj, const float4& q) {
+          const float ddx = pi.x - q.x, ddy = pi.y - q.y;
+          float dsq = __fmaf_rn(ddy, ddy, ddx * ddx);
+          if (DIM == 3) {
+            const float ddz = pi.z - q.z;
+            dsq = __fmaf_rn(ddz, ddz, dsq);
+          }
+          const float rc = base_r + q.w;
+          if (dsq < rc * rc && oj != oh) {
+            if (n < cap) out[n * 32] = (int32_t)((uint32_t)sslot[oj] | (simg[oj] != img_h ? 0x80000000u : 0u));
+            ++n;
+          }
+        };
+        int o = oa;
+        for (; o + 4 <= ob; o += 4) {
           float4 q[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) q[u] = spos[o + u < ob ? o + u : oh];
+          for (int u = 0; u < 4; ++u) q[u] = spos[o + u];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int oj = o + u;
-            const float ddx = pi.x - q[u].x, ddy = pi.y - q[u].y;
-            float dsq = __fmaf_rn(ddy, ddy, ddx * ddx);
-            if (DIM == 3) {
-              const float ddz = pi.z - q[u].z;
-              dsq = __fmaf_rn(ddz, ddz, dsq);
-            }
-            const float rc = base_r + q[u].w;
-            if (oj < ob && oj != oh && dsq < rc * rc) {
-              if (n < cap) out[n * 32] = (int32_t)((uint32_t)sslot[oj] | (simg[oj] != img_h ? 0x80000000u : 0u));
-              ++n;
-            }
-          }
+          for (int u = 0; u < 4; ++u) test(o + u, q[u]);
         }
+        for (; o < ob; ++o) test(o, spos[o]);
       }
     }
     if (n > cap) atomicOr(&b.ctl->status, ST_NL_OVERFLOW);
