@@ -182,12 +182,15 @@ def run_reference(args, rank, world):
 
 
 # -------------------------------------------------------------- ours
-def traffic_from_profile(workload):
-    """dram bytes per fused-kernel launch from the committed ncu summary, if any."""
+def traffic_from_profile(workload, n, skin):
+    """dram bytes per fused-kernel launch from the committed ncu summary, when it
+    was captured on this workload's size and skin; else None."""
     p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"  # written from an ncu capture
     if p.exists():
         try:
             d = json.loads(p.read_text())
+            if d.get("n") != n or abs(float(d.get("skin", -1.0)) - float(skin)) > 1e-3:
+                return None
             return d.get("dram_bytes_per_launch")
         except Exception:
             return None
@@ -272,7 +275,7 @@ def run_ours(args, rank, world, dist):
     B = BYTES_PER_PARTICLE_STEP[w.dim]
     peak, peak_kind = peaks()
     achieved = B * w.N / (force_avg_ms * 1e-3) / 1e9
-    traffic = traffic_from_profile(args.workload)
+    traffic = traffic_from_profile(args.workload, w.N, skin)
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
