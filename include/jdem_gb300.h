@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 4
+#define JDEM_ABI_VERSION 5
 
 enum {
   JDEM_OK = 0,
@@ -94,6 +94,8 @@ typedef struct {
   int32_t neighbor_list;        /* Verlet list built at each re-sort: 0 = on (capacity from the
                                    density), > 0 = on with this initial capacity, -1 = off */
   int32_t graph_mode;           /* 0: CUDA graphs whose re-sort kernels sit in conditional nodes;
+                                   systems of at most 32768 slots whose cooperative launch fits
+                                   run each chunk as one many-step kernel in a while node;
                                    1: plain graphs (re-sort kernels always launched, returning
                                    early when no re-sort is due; profilers can see every node);
                                    2: no graphs (direct launches) */
@@ -140,6 +142,8 @@ typedef struct {
   int64_t list_regrowths;    /* Verlet-list capacity doublings after a row overflowed */
   int32_t list_capacity;     /* entries per Verlet-list row (0: no list) */
   int32_t list_tiles;        /* cell bricks of the shared-memory list path (0: slot-order path) */
+  int32_t many_step;         /* 1: step chunks run as one cooperative launch of many steps (small systems) */
+  int32_t reserved;
 } JdemStats;
 
 /* ABI version of the loaded library (JDEM_ABI_VERSION). */

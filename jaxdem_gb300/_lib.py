@@ -127,6 +127,8 @@ class Stats(C.Structure):
         ("list_regrowths", C.c_int64),
         ("list_capacity", C.c_int32),
         ("list_tiles", C.c_int32),
+        ("many_step", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -81,6 +81,7 @@ void JdemHandle::dfree(void* p) {
 void JdemHandle::drop_graphs() {
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
   graphs.clear();
+  multi_used = false;
 }
 
 // Host restatement of the grid choice: binning cell = 2 r_max + skin, grown
@@ -760,6 +761,61 @@ int JdemHandle::capture_step_conditional(int mode, cudaGraphConditionalHandle hc
   return JDEM_OK;
 }
 
+// A chunk of nsteps MODE_STEP steps of a small system as one while node:
+// body = re-sort kernels (returning at once when nothing is due), list build,
+// and the cooperative many-step kernel, which runs steps until the chunk ends
+// or a re-sort is due and sets the while condition (jdem_multi.cu).
+int JdemHandle::capture_multi(long long nsteps, cudaGraphExec_t* ge) {
+  *ge = nullptr;
+  JDEM_CUDA_TRY(this, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaSuccess;
+  bool ok = false;
+  do {
+    launch_multi_init(b, (unsigned int)nsteps, stream);
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cg;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(stream, &cst, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) break;
+    cudaGraphConditionalHandle hw;
+    if ((e = cudaGraphConditionalHandleCreate(&hw, cg, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    cudaGraphNodeParams prm = {cudaGraphNodeTypeConditional};
+    prm.type = cudaGraphNodeTypeConditional;
+    prm.conditional.handle = hw;
+    prm.conditional.type = cudaGraphCondTypeWhile;
+    prm.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &prm)) != cudaSuccess) break;
+    cudaGraph_t body = prm.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+      break;
+    launch_rebuild(dim, b, any_free, side);
+    launch_nlbuild(dim, b, side);
+    const int lrc = launch_multi(dim, b, hw, side);
+    cudaGraph_t body_out;
+    const cudaError_t e2 = cudaStreamEndCapture(side, &body_out);
+    if (lrc || e2 != cudaSuccess) {
+      e = e2 != cudaSuccess ? e2 : cudaErrorNotSupported;
+      break;
+    }
+    if ((e = cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+        cudaSuccess)
+      break;
+    ok = true;
+  } while (false);
+  const cudaError_t ee = cudaStreamEndCapture(stream, &g);
+  if (ok && ee == cudaSuccess && g) ok = cudaGraphInstantiate(ge, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    *ge = nullptr;
+    cudaGetLastError();
+    return fail(JDEM_ERR_CUDA, std::string("many-step graph capture: ") + cudaGetErrorString(e));
+  }
+  return JDEM_OK;
+}
+
 int JdemHandle::run_graph(long long nsteps, int mode_last) {
   if (graph_mode == 2) {
     for (long long k = 0; k < nsteps; ++k) enqueue_step(k + 1 == nsteps ? mode_last : MODE_STEP);
@@ -771,6 +827,14 @@ int JdemHandle::run_graph(long long nsteps, int mode_last) {
   auto it = graphs.find(key);
   if (it == graphs.end()) {
     cudaGraphExec_t ge = nullptr;
+    if (use_conditional && use_multi && mode_last == MODE_STEP && !any_free && multi_eligible(dim, b, dev)) {
+      if (capture_multi(nsteps, &ge) != JDEM_OK) {
+        use_multi = false;  // the per-step graphs below
+        err.clear();
+      } else {
+        multi_used = true;
+      }
+    }
     for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
       bool cond = use_conditional && attempt == 0;
       cudaGraph_t g = nullptr;
@@ -892,6 +956,17 @@ int JdemHandle::sync_status() {
     bbox_pending = false;
   }
   if (c->status & ST_NONFINITE) return fail(JDEM_ERR_NONFINITE, "non-finite position or velocity");
+  if (c->status & ST_BARRIER_TIMEOUT) {
+    // the many-step kernel stopped early: leave it for the per-step graphs
+    use_multi = false;
+    drop_graphs();
+    unsigned int zero[2] = {0u, c->status & ~(unsigned int)ST_BARRIER_TIMEOUT};
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->bar_count, &zero[0], 4, cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->status, &zero[1], 4, cudaMemcpyHostToDevice, stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
+    sticky_status &= ~(unsigned int)ST_BARRIER_TIMEOUT;
+    return fail(JDEM_ERR_CUDA, "many-step kernel: a grid barrier timed out; the steps of that chunk are incomplete");
+  }
 
   return JDEM_OK;
 }
@@ -1181,6 +1256,8 @@ int jdem_stats(JdemHandle* h, JdemStats* out) {
   out->list_regrowths = h->nl_regrowths;
   out->list_capacity = h->b.nl_cap;
   out->list_tiles = h->b.n_tiles;
+  out->many_step = h->multi_used ? 1 : 0;
+  out->reserved = 0;
   return JDEM_OK;
 }
 

@@ -102,6 +102,8 @@ struct JdemHandle {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;     // captures the conditional re-sort bodies
   bool use_conditional = true;
+  bool use_multi = true;  // small systems: many steps per cooperative launch (jdem_multi.cu)
+  bool multi_used = false;  // a cached graph runs its steps as one cooperative many-step launch
   int graph_mode = 0;
   bool own_stream = false;
   void* h_status = nullptr;
@@ -134,6 +136,7 @@ struct JdemHandle {
   int reset_ctl();
   int upload(const JdemHostState* s, bool device_ptrs);
   void enqueue_step(int mode);
+  int capture_multi(long long nsteps, cudaGraphExec_t* ge);
   int capture_handle(cudaGraphConditionalHandle* hc);
   int capture_step_conditional(int mode, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle* next);
   int run_graph(long long nsteps, int mode_last);

@@ -610,8 +610,6 @@ __global__ void __launch_bounds__(128) k_force_small(Bufs b, int mode) {
   if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
 }
 
-// Systems of at most this many slots use k_force_small (8 lanes a slot).
-constexpr long long kSmallForceSlots = 32768;
 
 // -------------------------------------------------------------- rotation
 

@@ -22,6 +22,16 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
 int rebuild_kernel_count(bool any_free);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
+// Systems of at most this many slots use k_force_small (8 lanes a slot).
+constexpr long long kSmallForceSlots = 32768;
+// Many steps per launch for small systems (jdem_multi.cu): whether the handle
+// qualifies (few enough slots to keep every block of the cooperative launch
+// resident; not Cundall-Strack or clumps), the chunk's step count, and the
+// cooperative k_multi that sets the while condition hw.  launch_multi returns
+// nonzero when the launch fails.
+bool multi_eligible(int dim, const Bufs& b, int device);
+void launch_multi_init(const Bufs& b, unsigned int n, cudaStream_t st);
+int launch_multi(int dim, const Bufs& b, cudaGraphConditionalHandle hw, cudaStream_t st);
 // Cundall-Strack (jdem_cs.cu): force + torque kernel, then the integrating
 // kernel unless mode is MODE_FORCE_ONLY; the rotational first-step phase.
 void launch_cs(int dim, const Bufs& b, int mode, cudaStream_t st);

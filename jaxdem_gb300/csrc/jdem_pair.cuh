@@ -162,7 +162,8 @@ struct ContactSum {
 template <int DIM>
 __device__ __forceinline__ float integrate_particle(const Bufs& b, int mode, long long t, unsigned int sel,
                                                     unsigned int ps, const SysParams& sp, float4 pi, uint32_t tg,
-                                                    float4 v4, float* F) {
+                                                    float4 v4, float* F, float4* p_out = nullptr,
+                                                    float4* v_out = nullptr) {
   const int base_mode = mode & 7;
   if (base_mode == MODE_FORCE_ONLY) {
     b.frc[sel][t] = make_float4(F[0], F[1], F[2], 0.0f);
@@ -216,6 +217,8 @@ __device__ __forceinline__ float integrate_particle(const Bufs& b, int mode, lon
   }
   b.pos[ps ^ 1u][t] = make_float4(p[0], p[1], p[2], pi.w);
   b.vel[sel][t] = make_float4(v[0], v[1], v[2], m);
+  if (p_out) *p_out = make_float4(p[0], p[1], p[2], pi.w);  // the values just stored
+  if (v_out) *v_out = make_float4(v[0], v[1], v[2], m);
   if (!(d2max == d2max) || d2max > 3.0e38f) {
     atomicOr(&b.ctl->status, ST_NONFINITE);
     d2max = 0.0f;
