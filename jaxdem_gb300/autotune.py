@@ -20,7 +20,9 @@ from typing import Callable, Optional, Sequence
 
 import numpy as np
 
-CANDIDATES = (0.15, 0.3, 0.45, 0.65, 0.9, 1.2)  # in units of r_max
+# in units of r_max; the large skins pay off for small systems, whose steps
+# cost little next to a re-sort (many-step launches)
+CANDIDATES = (0.15, 0.3, 0.45, 0.65, 0.9, 1.2, 1.6, 2.0)
 CACHE = Path(os.environ.get("JDEM_TUNE_CACHE", Path.home() / ".cache" / "jaxdem_gb300" / "tune.json"))
 
 

@@ -960,9 +960,12 @@ int JdemHandle::sync_status() {
     // the many-step kernel stopped early: leave it for the per-step graphs
     use_multi = false;
     drop_graphs();
-    unsigned int zero[2] = {0u, c->status & ~(unsigned int)ST_BARRIER_TIMEOUT};
-    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->bar_count, &zero[0], 4, cudaMemcpyHostToDevice, stream));
-    JDEM_CUDA_TRY(this, cudaMemcpyAsync(&b.ctl->status, &zero[1], 4, cudaMemcpyHostToDevice, stream));
+    Ctl fresh = *c;  // barrier bookkeeping back to zero, the timeout bit cleared
+    fresh.status &= ~(unsigned int)ST_BARRIER_TIMEOUT;
+    fresh.bar_count = fresh.bar_base = fresh.mstep = 0u;
+    fresh.mx[0] = fresh.mx[1] = fresh.mx[2] = 0u;
+    std::memcpy(h_status, &fresh, sizeof(Ctl));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.ctl, h_status, sizeof(Ctl), cudaMemcpyHostToDevice, stream));
     JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
     sticky_status &= ~(unsigned int)ST_BARRIER_TIMEOUT;
     return fail(JDEM_ERR_CUDA, "many-step kernel: a grid barrier timed out; the steps of that chunk are incomplete");

@@ -26,25 +26,32 @@ namespace {
 constexpr int kMultiG = 8;          // lanes per slot (as k_force_small)
 constexpr int kMultiT = 128;        // threads per block
 constexpr int kMultiE = 4;          // list entries a lane keeps in registers (row entries g, g + 8, ...)
-constexpr unsigned int kBarrierSpins = 1u << 21;  // polls (with a short sleep) before a barrier gives up
+constexpr int kMultiMaxSys = 8;     // systems of a handle that takes the many-step path
+constexpr unsigned int kBarrierSpins = 1u << 21;  // polls of the arrival count (about a second) before a barrier gives up
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
+__device__ __forceinline__ void red_release_add(unsigned int* p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 __device__ __forceinline__ float4 ldc4(const float4* p) { return __ldcg(p); }
 
-// Grid barrier of a cooperative launch that also reduces the step's largest
+// Grid barrier of a cooperative launch that also reduces step s's largest
 // squared drift.  Thread 0 of each block folds its warps' maxima (s_wmax)
-// into ctl->mx, then arrives; the last block to arrive takes and clears
-// ctl->mx and publishes it with the new generation in one 64-bit word, so
-// the waiting blocks read both with one load.  Bounded: a block that polls
-// kBarrierSpins times without seeing its generation records
-// ST_BARRIER_TIMEOUT and returns false.  gen (thread 0 of each block) is the
-// generation this block last passed.
-__device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& gen, const float* s_wmax, float& m2) {
+// into ctl->mx[s % 3] and arrives with one release add on the never-reset
+// arrival count; every block then polls the count until it reaches its
+// target (the launch's base plus gridDim.x per barrier), takes an acquire
+// fence and reads the slot.  Bounded: a block that polls kBarrierSpins times
+// records ST_BARRIER_TIMEOUT and returns false.
+__device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& target, unsigned int s,
+                                                 const float* s_wmax, float& m2) {
   __shared__ int s_ok;
   __shared__ unsigned int s_m2;
   __syncthreads();
@@ -52,34 +59,22 @@ __device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& gen, co
     float bmax = 0.0f;
 #pragma unroll
     for (int w = 0; w < kMultiT / 32; ++w) bmax = fmaxf(bmax, s_wmax[w]);
-    if (bmax > 0.0f) atomicMax(&ctl->mx, __float_as_uint(bmax));
+    unsigned int* slot = &ctl->mx[s % 3u];
+    if (bmax > 0.0f) atomicMax(slot, __float_as_uint(bmax));
+    red_release_add(&ctl->bar_count, 1u);
+    target += gridDim.x;
     int ok = 1;
-    const unsigned int target = gen + 1u;
-    unsigned long long word = 0ull;
-    __threadfence();
-    if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1u) {
-      atomicExch(&ctl->bar_count, 0u);
-      const unsigned int mx = atomicExch(&ctl->mx, 0u);
-      word = ((unsigned long long)mx << 32) | target;
-      __threadfence();
-      atomicExch(&ctl->bar_word, word);
-    } else {
-      unsigned int spins = 0;
-      for (;;) {
-        word = ld_acquire_u64(&ctl->bar_word);
-        if ((unsigned int)word == target) break;
-        if (++spins > kBarrierSpins) {
-          atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
+    unsigned int spins = 0;
+    while ((int)(ld_relaxed_u32(&ctl->bar_count) - target) < 0) {
+      if (++spins > kBarrierSpins) {
+        atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
+        ok = 0;
+        break;
       }
     }
-    __threadfence();
-    gen = target;
+    fence_acquire();
     s_ok = ok;
-    s_m2 = (unsigned int)(word >> 32);
+    s_m2 = ld_relaxed_u32(slot);
   }
   __syncthreads();
   m2 = __uint_as_float(s_m2);
@@ -108,20 +103,27 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
     return;
   }
   __shared__ float s_wmax[kMultiT / 32];
-  unsigned int gen = 0u;
-  if (threadIdx.x == 0) gen = (unsigned int)ld_acquire_u64(&ctl->bar_word);
+  // arrivals counted when the previous launch ended (every block of it had arrived)
+  unsigned int target = ld_cg_u32(&ctl->bar_base);
+  unsigned int s = ld_cg_u32(&ctl->mstep);
   const unsigned int sel = ld_cg_u32(&ctl->sel);
   unsigned int ps = ld_cg_u32(&ctl->pos_sel);
   const bool use_list = b.nl_cap > 0 && (ld_cg_u32(&ctl->status) & ST_NL_OVERFLOW) == 0u;
   float bound = __ldcg(&ctl->bound);
   const float skin_half = __ldcg(&ctl->skin_half);
 
+  // The system table in shared memory: the acquire fence of every barrier
+  // drops L1, and the integrator reads the system's fields every step.
+  __shared__ SysParams s_sys[kMultiMaxSys];
+  for (int i = threadIdx.x; i < b.S; i += kMultiT) s_sys[i] = b.sys[i];
+  __syncthreads();
+
   const long long t = (blockIdx.x * (long long)kMultiT + threadIdx.x) / G;
   const int lane = threadIdx.x & 31, g = lane % G, base = lane - g;
   const bool live = t < b.P;
   uint32_t tg = 0u;
   int n = 0;
-  const SysParams* spp = b.sys;
+  const SysParams* spp = &s_sys[0];
   float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), v4 = pi;
   const int32_t* nb = nullptr;
   uint32_t ent[kMultiE];
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
   for (int i = 0; i < kMultiE; ++i) ent[i] = 0u;
   if (live) {
     tg = b.tag[sel][t];
-    spp = &b.sys[tg & TAG_SYS_MASK];
+    spp = &s_sys[tg & TAG_SYS_MASK];
     pi = ldc4(&b.pos[ps][t]);
     if (g == 0) v4 = ldc4(&b.vel[sel][t]);
     if (use_list) {
@@ -143,12 +145,16 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
     }
   }
 
+  // per-slot material constants, read once
+  ContactSum<DIM, GENERAL, LAW> acc(b, *spp, pi, tg, sel, live ? t : 0);
+
   bool ok = true;
   for (;;) {
     float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
     if (live) {
       const float4* P = b.pos[ps];
-      ContactSum<DIM, GENERAL, LAW> acc(b, *spp, pi, tg, sel, t);
+      acc.fx = acc.fy = acc.fz = acc.ex = acc.ey = acc.ez = 0.0f;
+      acc.pi = pi;
       if (use_list) {
         float4 q[kMultiE];
 #pragma unroll
@@ -205,15 +211,20 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
     d2 = warp_max(d2);
     if (lane == 0) s_wmax[threadIdx.x >> 5] = d2;
     float m2;
-    ok = grid_barrier_max(ctl, gen, s_wmax, m2);
+    ok = grid_barrier_max(ctl, target, s, s_wmax, m2);
     if (!ok) break;
     // k_fin: bound += sqrt(max squared drift); positions flip
     bound = bound + sqrtf(m2);
     ps ^= 1u;
     --left;
+    // the slot of step s + 2 was last read, by every block, before this barrier
+    if (lead) ctl->mx[(s + 2u) % 3u] = 0u;
+    ++s;
     if (bound > skin_half || left == 0u) break;
   }
   if (lead) {
+    ctl->bar_base = target;
+    ctl->mstep = s;
     ctl->bound = bound;
     ctl->pos_sel = ps;
     ctl->nl_dirty = 0u;
@@ -256,7 +267,7 @@ bool multi_general(const Bufs& b) { return b.n_mat > 1 || (b.bond_w > 0 && !b.in
 }  // namespace
 
 bool multi_eligible(int dim, const Bufs& b, int device) {
-  if (b.P <= 0 || b.P > kSmallForceSlots || b.NC || b.law == LAW_CS) return false;
+  if (b.P <= 0 || b.P > kSmallForceSlots || b.NC || b.law == LAW_CS || b.S > kMultiMaxSys) return false;
   int sms = 0, coop = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess) {
