@@ -86,6 +86,31 @@ def test_short_chunks_and_single_steps():
         assert np.array_equal(a[k], b[k]), k
 
 
+def test_several_systems_bit_identical():
+    """Three periodic boxes of different sizes and densities in one handle (the system
+    table the many-step kernel keeps in shared memory)."""
+    rng = np.random.Generator(np.random.PCG64(77))
+    ws = [W.periodic_system(f"s{i}", rng, n, 3, rng.choice([0.5, 0.6], size=n), phi, 0.3, 1e-3, 10)
+          for i, (n, phi) in enumerate([(1500, 0.35), (700, 0.5), (2300, 0.42)])]
+    cat = lambda k: np.concatenate([getattr(w, k) for w in ws])
+    young = np.array([[W.K_SPRING]], np.float32)
+    outs, sts = [], []
+    for mode in (0, 2):
+        eng = Engine(3, [w.desc() for w in ws], young, skin=0.03, graph_mode=mode)
+        try:
+            eng.upload(pos=cat("pos"), rad=cat("rad"), mass=cat("mass"), vel=cat("vel"))
+            eng.step(150)
+            eng.step(73)
+            outs.append(eng.download())
+            sts.append(eng.stats())
+        finally:
+            eng.close()
+    assert sts[0]["many_step"] == 1 and sts[1]["many_step"] == 0
+    assert sts[0]["rebuilds"] == sts[1]["rebuilds"] > 2
+    for k in ("pos_c", "vel", "force"):
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
 def test_large_system_keeps_per_step_graphs():
     w = W.c1(N=40000, seed=76)
     _, st = run(w, np.array([[W.K_SPRING]], np.float32), 0, (60,), 0.1)
