@@ -325,8 +325,8 @@ __global__ void k_gather(Bufs b) {
   long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   if (u < b.P) {
-    int t = b.perm_tmp[u];
-    const float4 p = b.pos[ps][t];
+    int t = __ldcs(&b.perm_tmp[u]);  // old-order records are read once: streaming loads
+    const float4 p = __ldcs(&b.pos[ps][t]);
     b.pos[ps ^ 1u][u] = p;
     if (b.posw) {
       // positions wrapped into the primary box and the image they came from,
@@ -350,12 +350,12 @@ __global__ void k_gather(Bufs b) {
       b.posw[u] = w;
       if (b.img) b.img[u] = im;
     }
-    b.vel[sel ^ 1u][u] = b.vel[sel][t];
+    b.vel[sel ^ 1u][u] = __ldcs(&b.vel[sel][t]);
     // forces are not moved: every re-sort is followed by a force kernel that
     // rewrites frc for all slots before anything reads it
     b.tag[sel ^ 1u][u] = b.tag[sel][t];
-    b.orig[sel ^ 1u][u] = b.orig[sel][t];
-    b.key[sel ^ 1u][u] = b.key_tmp[t];
+    b.orig[sel ^ 1u][u] = __ldcs(&b.orig[sel][t]);
+    b.key[sel ^ 1u][u] = __ldcs(&b.key_tmp[t]);
   }
 }
 
