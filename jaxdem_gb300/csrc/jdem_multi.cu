@@ -25,7 +25,7 @@ namespace {
 
 constexpr int kMultiG = 8;          // lanes per slot (as k_force_small)
 constexpr int kMultiT = 128;        // threads per block
-constexpr int kMultiE = 4;          // list entries a lane keeps in registers (row entries g, g + 8, ...)
+constexpr int kMultiE = 6;          // list entries a lane keeps in registers (row entries g, g + 8, ...; rows up to 48)
 constexpr int kMultiMaxSys = 8;     // systems of a handle that takes the many-step path
 constexpr unsigned int kBarrierSpins = 1u << 21;  // polls of the arrival count (about a second) before a barrier gives up
 
