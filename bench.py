@@ -330,7 +330,10 @@ def run_ours(args, rank, world, dist):
                                    "regrowths": stats["list_regrowths"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_force (fused force + integrate)", "bytes_per_unit": B,
+                     "kernel": ("k_force_small (8 lanes a slot), timed per launch: the timed region runs the "
+                                "same step inside cooperative many-step launches (k_multi)")
+                     if stats.get("many_step") else "k_force (fused force + integrate)",
+                     "bytes_per_unit": B,
                      "avg_launch_ms": force_avg_ms},
         "cpu_baseline": cpu,
         "e2e": e2e,
