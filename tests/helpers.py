@@ -19,6 +19,15 @@ def force_err(gpu, ref):
     return float((np.linalg.norm(gpu - ref, axis=-1) / np.maximum(na, floor)).max()) if na.size else 0.0
 
 
+def global_force_err(gpu, ref):
+    """||F_gpu - F_ref||_2 / ||F_ref||_2 over all particles, float64 norms (0 without forces).
+    The per-particle floored bar of force_err implies the same bar here."""
+    ref = np.asarray(ref, np.float64)
+    gpu = np.asarray(gpu, np.float64)
+    nr = np.linalg.norm(ref)
+    return float(np.linalg.norm(gpu - ref) / nr) if nr > 0 else 0.0
+
+
 def min_image_diff(a, b, box=None):
     d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
     if box is not None:

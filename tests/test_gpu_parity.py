@@ -19,7 +19,7 @@ import oracle
 from jaxdem_gb300 import workloads as W
 from jaxdem_gb300._lib import Engine
 from oracle import dem_ref as R
-from tests.helpers import force_err, min_image_diff, osystem, ostate
+from tests.helpers import force_err, global_force_err, min_image_diff, osystem, ostate
 
 pytestmark = pytest.mark.gpu
 
@@ -83,8 +83,10 @@ def test_compute_force_matches_oracle(case):
         eng.close()
     e64 = force_err(out["force"], ref64)
     e32 = force_err(out["force"], ref32)
+    g64 = global_force_err(out["force"], ref64)
     assert e64 <= 1e-5, f"{case}: err vs float64-accumulated oracle {e64}"
     assert e32 <= 1e-5, f"{case}: err vs float32 reference-order oracle {e32}"
+    assert g64 <= 1e-5, f"{case}: ||dF|| / ||F|| vs float64-accumulated oracle {g64}"
     assert np.all(out["torque"] == 0)
 
 
