@@ -108,7 +108,7 @@ def _bidisperse(rng, N):
 def c2(N: int = 1 << 20, seed: int = 2) -> Workload:
     rng = np.random.Generator(np.random.PCG64(seed))
     rad = _bidisperse(rng, N)
-    # jitter of 1e-3 of the reference cell edge 2 * 0.7 (BASELINE recipe)
+    # jitter of 1e-3 of the reference cell edge 2 * 0.7
     return periodic_system("c2", rng, N, 3, rad, 0.55, 0.05, 5e-4, 200, jitter=1e-3 * 1.4)
 
 
