@@ -1028,8 +1028,6 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st) {
   k_sort_fin<<<1, 1, 0, st>>>(b.ctl);
 }
 
-int rebuild_kernel_count(bool any_free) { return any_free ? 9 : 8; }
-
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
   if (dim == 3) k_pre<3><<<nblk(b.P, 256), 256, 0, st>>>(b, mode);

@@ -19,7 +19,6 @@ void launch_segcopy(const long long* seg, int nseg, int narr, const float* const
                     const int* width, cudaStream_t st);
 void launch_scan(const Bufs& b, cudaStream_t st);
 void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
-int rebuild_kernel_count(bool any_free);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
 // Systems of at most this many slots use k_force_small (8 lanes a slot).
