@@ -238,13 +238,17 @@ def run_ours(args, rank, world, dist):
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
-    # warm-up steps (graph capture, first re-sort)
-    for _ in range(max(args.warmup, 1)):
-        eng.step(1)
-    eng.step(CHUNK)
-
     K = args.steps
     chunks = [CHUNK] * (K // CHUNK) + ([K % CHUNK] if K % CHUNK else [])
+    # warm-up steps: the first re-sort, then one call of every chunk length the timed
+    # region runs, so that every CUDA graph it launches is captured and instantiated
+    # before the first timing event (a call of c steps launches the graphs of c - 1
+    # steps and of the final step)
+    for _ in range(max(args.warmup, 1)):
+        eng.step(1)
+    for c in sorted(set(chunks)):
+        eng.step(c)
+    graphs_before = eng.stats()["graphs"]
     torch.cuda.synchronize()
     rebuilds_before = eng.stats()["rebuilds"]
     if dist is not None:
@@ -269,6 +273,8 @@ def run_ours(args, rank, world, dist):
     clk = clocks.stop()
     total_ms = replicas.max_over_ranks(dist, total_ms, device=f"cuda:{dev}")
     stats = eng.stats()
+    # no graph may be captured inside the timed region
+    graphs_captured_timed = stats["graphs"] - graphs_before
 
     # instrumented pass: per-launch events around the fused force kernel
     tot_ms, force_ms = eng.step_timed(CHUNK)
@@ -306,13 +312,15 @@ def run_ours(args, rank, world, dist):
             host_register(a)
         e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
         e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
-        e2e_eng.step(CHUNK)  # capture graphs once, outside the timed region
+        e2e_eng.step(K)  # the timed call sequence once: every graph it launches is captured here
+        e2e_graphs = e2e_eng.stats()["graphs"]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
         e2e_eng.step(K)
         e2e_eng.download(outb)
         e2e_s = time.perf_counter() - t0
+        e2e_new_graphs = e2e_eng.stats()["graphs"] - e2e_graphs
         for a in list(host.values()) + list(outb.values()):
             host_unregister(a)
         e2e_eng.close()
@@ -320,6 +328,7 @@ def run_ours(args, rank, world, dist):
         d2h = sum(a.nbytes for a in outb.values())
         e2e = {"value": world * w.N * K / e2e_s, "unit": "particle-steps/s",
                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+               "graphs_captured_in_timed_region": e2e_new_graphs,
                "note": f"one C-ABI call sequence per {K} steps: upload (pinned host), step, download"}
 
     cpu = None
@@ -346,6 +355,7 @@ def run_ours(args, rank, world, dist):
                    "l2": "flushed (256 MB write) between timed 50-step chunks",
                    "parallelism": "replicas" if world > 1 else "single",
                    "resorts_in_timed_region": rebuilds_timed,
+                   "graphs_captured_in_timed_region": graphs_captured_timed,
                    "verlet_list": {"capacity": stats["list_capacity"], "tiles": stats["list_tiles"],
                                    "regrowths": stats["list_regrowths"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

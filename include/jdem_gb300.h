@@ -21,8 +21,9 @@
  * Conventions.  Every function returns an int status (JDEM_OK = 0).  No C++
  * exception crosses this boundary.  A handle owns its device memory, which
  * stays resident between calls; host buffers belong to the caller.  All work
- * is ordered on the handle's stream.  A handle is not internally locked: use
- * one handle per host thread.  Arrays use the reference's row-major layouts:
+ * is ordered on the handle's active stream: its own stream, or the caller's
+ * after jdem_set_stream.  A handle is not internally locked: use one handle
+ * per host thread.  Arrays use the reference's row-major layouts:
  * pos_c/vel/force (N, dim), q (N, 4) as (w, x, y, z), ang_vel/torque/inertia
  * (N, 1) in 2D or (N, 3) in 3D, bond_id (N, W) padded with -1.  With several
  * systems in one handle their particles are concatenated in system order.
@@ -37,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 5
+#define JDEM_ABI_VERSION 6
 
 enum {
   JDEM_OK = 0,
@@ -240,8 +241,31 @@ int jdem_neighbor_list(JdemHandle* h, float cutoff, int32_t max_neighbors, int32
 int jdem_domain_state(JdemHandle* h, float* box, float* anchor);
 
 int jdem_stats(JdemHandle* h, JdemStats* out);
-/* cudaStream_t the handle launches on (as void*). */
+/* Particle count and dimension of the handle's system list, without touching
+ * the device (jdem_stats first reads the device status, which waits for the
+ * handle's stream). */
+int jdem_shape(const JdemHandle* h, int64_t* n_particles, int32_t* dim);
+/* cudaStream_t the handle launches on (as void*): its own stream, or the one
+ * given to jdem_set_stream. */
 void* jdem_stream(JdemHandle* h);
+
+/* Stream-ordered use, as an XLA FFI handler needs it (the reference's System.step
+ * and compute_force, system.py:701-748 and colliders/cell_list.py:434-464, are
+ * functional and XLA orders them on its compute stream): queue every later call's
+ * work on `stream` (a cudaStream_t of the handle's device, as void*; NULL returns
+ * to the handle's own stream).  Work already queued on the previous stream is
+ * ordered before the next stream's work by an event, without a host wait.  CUDA
+ * graphs are still captured on the handle's own stream and launched on `stream`.
+ * Afterwards jdem_upload_device reads the caller's arrays after everything the
+ * caller queued on `stream` before the call; it waits on the host once, for the
+ * eight-word per-system summary (maximum radius, bounding box, input checks) that
+ * sizes the cell grid.  jdem_step_async and jdem_download_device_async queue
+ * their work and return; the results are valid for later work on `stream`. */
+int jdem_set_stream(JdemHandle* h, void* stream);
+/* jdem_download_device without the host wait: the copies into the caller's
+ * device arrays are queued on the active stream; device status bits are read
+ * by the next jdem_sync / jdem_step / jdem_stats. */
+int jdem_download_device_async(JdemHandle* h, JdemHostState* dev);
 
 /* Contact forces of one sphere system from caller-owned device buffers, without
  * allocating device memory.  No counterpart in the reference: it exists for callers

@@ -158,6 +158,9 @@ _PROTOS = [
     ("jdem_domain_state", [C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     ("jdem_stats", [C.c_void_p, C.POINTER(Stats)], C.c_int),
     ("jdem_stream", [C.c_void_p], C.c_void_p),
+    ("jdem_set_stream", [C.c_void_p, C.c_void_p], C.c_int),
+    ("jdem_shape", [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
+    ("jdem_download_device_async", [C.c_void_p, C.POINTER(HostState)], C.c_int),
     ("jdem_host_register", [C.c_void_p, C.c_size_t], C.c_int),
     ("jdem_host_unregister", [C.c_void_p], C.c_int),
 ]
@@ -443,6 +446,37 @@ class Engine:
 
     def stream(self) -> int:
         return int(self.lib.jdem_stream(self.h) or 0)
+
+    def set_stream(self, stream: int) -> None:
+        """Queue later work on ``stream`` (a ``cudaStream_t`` as an int, e.g.
+        ``torch.cuda.Stream().cuda_stream``); 0 returns to the handle's own stream."""
+        self._check(self.lib.jdem_set_stream(self.h, C.c_void_p(int(stream)) if stream else None))
+
+    _DEVICE_FIELDS = ("pos_c", "vel", "force", "q", "ang_vel", "torque", "rad", "mass", "inertia", "mat_id",
+                      "fixed", "bond_id", "pos_p", "clump_id")
+
+    def _device_state(self, arrays: dict) -> HostState:
+        hs = HostState()
+        for k, a in arrays.items():
+            if k not in self._DEVICE_FIELDS:
+                raise ValueError(f"unknown state field {k!r}")
+            if a is None:
+                continue
+            if not hasattr(a, "data_ptr") or not a.is_cuda or not a.is_contiguous():
+                raise ValueError(f"{k}: expected a contiguous CUDA tensor")
+            setattr(hs, k, a.data_ptr())
+        return hs
+
+    def upload_device(self, **arrays) -> None:
+        """``jdem_upload_device`` from contiguous CUDA tensors in the reference layout
+        (float32; int32 ``mat_id``/``bond_id``/``clump_id``, uint8 ``fixed``)."""
+        self._check(self.lib.jdem_upload_device(self.h, C.byref(self._device_state(arrays))))
+
+    def download_device(self, wait: bool = True, **arrays) -> None:
+        """Copy pos_c / vel / force / q / ang_vel / torque into CUDA tensors; with
+        ``wait=False`` the copies are only queued on the active stream."""
+        fn = self.lib.jdem_download_device if wait else self.lib.jdem_download_device_async
+        self._check(fn(self.h, C.byref(self._device_state(arrays))))
 
 
 def host_register(a: np.ndarray) -> None:

@@ -4,6 +4,10 @@
 links ``_lib/libjdem_gb300.so``.  Flags: ``-fmad=false`` keeps each float
 product and sum rounding as written (the kernels restate the reference's
 float32 operation order); ``-lineinfo`` for profiler source correlation.
+
+The XLA FFI handlers (``csrc/ffi/jdem_xla_ffi.cc``) are built into
+``_lib/libjdem_xla_ffi.so`` only where jaxlib's FFI headers exist: the
+directory named by ``JDEM_JAX_INCLUDE``, else ``jax.ffi.include_dir()``.
 """
 
 from __future__ import annotations
@@ -72,7 +76,46 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_xla_ffi(LIB)
     return LIB
+
+
+def jax_ffi_include() -> Path | None:
+    """Directory holding ``xla/ffi/api/ffi.h`` (jaxlib), or None when jaxlib is absent."""
+    env = os.environ.get("JDEM_JAX_INCLUDE")
+    cands = [Path(env)] if env else []
+    if not env:
+        try:
+            import jax.ffi  # noqa: PLC0415
+
+            cands.append(Path(jax.ffi.include_dir()))
+        except Exception:
+            pass
+    for c in cands:
+        if (c / "xla" / "ffi" / "api" / "ffi.h").exists():
+            return c
+    return None
+
+
+FFI_SRC = CSRC / "ffi" / "jdem_xla_ffi.cc"
+FFI_LIB = OUT_DIR / "libjdem_xla_ffi.so"
+
+
+def build_xla_ffi(lib: Path = LIB) -> Path | None:
+    """Build the XLA FFI handler library against ``lib`` when jaxlib's headers are
+    found; returns its path, or None (nothing to build against)."""
+    inc_jax = jax_ffi_include()
+    if inc_jax is None:
+        return None
+    if FFI_LIB.exists() and FFI_LIB.stat().st_mtime >= max(FFI_SRC.stat().st_mtime, lib.stat().st_mtime):
+        return FFI_LIB
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-x", "cu",
+           "-I", str(PKG.parent / "include"), "-I", str(inc_jax), str(FFI_SRC), "-o", str(FFI_LIB),
+           "-L", str(OUT_DIR), "-ljdem_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"XLA FFI handler build failed:\n{r.stdout}\n{r.stderr}")
+    return FFI_LIB
 
 
 if __name__ == "__main__":

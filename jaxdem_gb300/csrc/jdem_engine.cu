@@ -44,8 +44,9 @@ void JdemHandle::free_all() {
   device_bytes = 0;
   if (h_status) cudaFreeHost(h_status);
   h_status = nullptr;
-  if (own_stream && stream) cudaStreamDestroy(stream);
+  if (own) cudaStreamDestroy(own);
   if (side) cudaStreamDestroy(side);
+  own = nullptr;
   stream = nullptr;
   side = nullptr;
   for (auto& e : ev_pool) cudaEventDestroy(e);
@@ -154,9 +155,9 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   nl_request = cfg->neighbor_list;
   int rc0 = set_systems(cfg->systems, S);
   if (rc0) return rc0;
-  JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-  own_stream = true;
+  stream = own;
   JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, 64));
   int rc;
   if ((rc = dalloc((void**)&b.ctl, sizeof(Ctl)))) return rc;
@@ -475,7 +476,9 @@ int JdemHandle::plan_tiles() {
       tiles_alloc = (long long)t.size();
     }
     if (!t.empty())
-      JDEM_CUDA_TRY(this, cudaMemcpy(d_tiles, t.data(), sizeof(TileDesc) * t.size(), cudaMemcpyHostToDevice));
+      JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tiles, t.data(), sizeof(TileDesc) * t.size(), cudaMemcpyHostToDevice,
+                                          stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));  // t is freed on return
     tiles_h.swap(t);
   }
   b.tiles = d_tiles;
@@ -624,7 +627,10 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
     auto host_view = [&](const float* src, size_t count, std::vector<float>& tmp) -> const float* {
       if (!device_ptrs) return src;
       tmp.resize(count);
-      if (cudaMemcpy(tmp.data(), src, count * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return nullptr;
+      // on the active stream: ordered after the caller's work that produced src
+      if (cudaMemcpyAsync(tmp.data(), src, count * 4, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+          cudaStreamSynchronize(stream) != cudaSuccess)
+        return nullptr;
       return tmp.data();
     };
     std::vector<float> tmp;
@@ -826,6 +832,15 @@ int JdemHandle::run_graph(long long nsteps, int mode_last) {
   long long key = nsteps * 64 + mode_last;
   auto it = graphs.find(key);
   if (it == graphs.end()) {
+    // Graphs are captured on the handle's own stream, which has no pending
+    // work of the caller's, and launched on the active stream (possibly the
+    // caller's) below; the capture only records work, it runs nothing.
+    struct Restore {
+      cudaStream_t& ref;
+      cudaStream_t saved;
+      ~Restore() { ref = saved; }
+    } restore{stream, stream};
+    stream = own;
     cudaGraphExec_t ge = nullptr;
     if (use_conditional && use_multi && mode_last == MODE_STEP && !any_free && multi_eligible(dim, b, dev)) {
       if (capture_multi(nsteps, &ge) != JDEM_OK) {
@@ -938,7 +953,9 @@ int JdemHandle::sync_status() {
   if (bbox_pending) {
     // FreeDomain.apply of the last step: box = max - min, anchor = min (free.py:59-63)
     std::vector<unsigned int> bb((size_t)S * 6);
-    JDEM_CUDA_TRY(this, cudaMemcpy(bb.data(), b.bbox, sizeof(unsigned int) * S * 6, cudaMemcpyDeviceToHost));
+    JDEM_CUDA_TRY(this, cudaMemcpyAsync(bb.data(), b.bbox, sizeof(unsigned int) * S * 6, cudaMemcpyDeviceToHost,
+                                        stream));
+    JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
     auto dec = [](unsigned int u) {
       unsigned int v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
       float f;
@@ -1024,7 +1041,7 @@ int JdemHandle::step_timed(long long n, double* total_ms, double* force_ms) {
   return sync_status();
 }
 
-int JdemHandle::download(JdemHostState* s, bool device_ptrs) {
+int JdemHandle::download(JdemHostState* s, bool device_ptrs, bool wait) {
   if (!uploaded) return fail(JDEM_ERR_NOT_READY, "download before upload");
   if (!s) return fail(JDEM_ERR_BAD_ARG, "download: null state");
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
@@ -1042,7 +1059,22 @@ int JdemHandle::download(JdemHostState* s, bool device_ptrs) {
     if (s->ang_vel) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->ang_vel, d_w, N * ad * 4, kind, stream));
     if (s->torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(s->torque, d_tq, N * ad * 4, kind, stream));
   }
-  return sync_status();
+  return wait ? sync_status() : JDEM_OK;
+}
+
+int JdemHandle::set_stream(void* s) {
+  JDEM_CUDA_TRY(this, cudaSetDevice(dev));
+  cudaStream_t next = s ? (cudaStream_t)s : own;
+  if (next == stream) return JDEM_OK;
+  // work queued on the previous stream comes before anything queued on the next one
+  cudaEvent_t ev;
+  JDEM_CUDA_TRY(this, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(next, ev, 0);
+  cudaEventDestroy(ev);
+  JDEM_CUDA_TRY(this, e);
+  stream = next;
+  return JDEM_OK;
 }
 
 int JdemHandle::compute_force() {
@@ -1172,6 +1204,7 @@ int jdem_destroy(JdemHandle* h) {
   if (!h) return JDEM_ERR_BAD_ARG;
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->own && h->own != h->stream) cudaStreamSynchronize(h->own);
   h->free_all();
   delete h;
   return JDEM_OK;
@@ -1208,6 +1241,12 @@ int jdem_download(JdemHandle* h, JdemHostState* s) {
 }
 int jdem_download_device(JdemHandle* h, JdemHostState* s) {
   return h ? jdem_guard(&h->err, [&] { return h->download(s, true); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_download_device_async(JdemHandle* h, JdemHostState* s) {
+  return h ? jdem_guard(&h->err, [&] { return h->download(s, true, false); }) : JDEM_ERR_BAD_ARG;
+}
+int jdem_set_stream(JdemHandle* h, void* stream) {
+  return h ? jdem_guard(&h->err, [&] { return h->set_stream(stream); }) : JDEM_ERR_BAD_ARG;
 }
 int jdem_compute_force(JdemHandle* h) {
   return h ? jdem_guard(&h->err, [&] { return h->compute_force(); }) : JDEM_ERR_BAD_ARG;
@@ -1265,6 +1304,13 @@ int jdem_stats(JdemHandle* h, JdemStats* out) {
 }
 
 void* jdem_stream(JdemHandle* h) { return h ? (void*)h->stream : nullptr; }
+
+int jdem_shape(const JdemHandle* h, int64_t* n_particles, int32_t* dim) {
+  if (!h || !n_particles || !dim) return JDEM_ERR_BAD_ARG;
+  *n_particles = h->P;
+  *dim = h->dim;
+  return JDEM_OK;
+}
 
 int jdem_host_register(void* ptr, size_t bytes) {
   if (!ptr || bytes == 0) return JDEM_ERR_BAD_ARG;

@@ -99,13 +99,13 @@ struct JdemHandle {
   size_t d_frames_bytes = 0;
 
   // runtime
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // active stream: own, or the caller's (jdem_set_stream)
   cudaStream_t side = nullptr;     // captures the conditional re-sort bodies
   bool use_conditional = true;
   bool use_multi = true;  // small systems: many steps per cooperative launch (jdem_multi.cu)
   bool multi_used = false;  // a cached graph runs its steps as one cooperative many-step launch
   int graph_mode = 0;
-  bool own_stream = false;
+  cudaStream_t own = nullptr;  // created by the handle: graph captures, and the default active stream
   void* h_status = nullptr;
   std::map<long long, cudaGraphExec_t> graphs;
   std::vector<cudaEvent_t> ev_pool;
@@ -143,7 +143,8 @@ struct JdemHandle {
   int step_async(long long n);
   int sync_status();
   int step_timed(long long n, double* total_ms, double* force_ms);
-  int download(JdemHostState* s, bool device_ptrs);
+  int download(JdemHostState* s, bool device_ptrs, bool wait = true);
+  int set_stream(void* s);
   int compute_force();
   int energy(double* out, bool per_system);
   int contacts(int32_t* pairs, long long cap, long long* count);

@@ -607,7 +607,9 @@ int JdemHandle::setup_clumps(const JdemHostState* s, bool device_ptrs) {
       std::memcpy(dst, src, bytes);
       return true;
     }
-    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess;
+    // on the active stream: ordered after the caller's work that produced src
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream) == cudaSuccess &&
+           cudaStreamSynchronize(stream) == cudaSuccess;
   };
   if (s->clump_id) {
     if (!fetch(cid.data(), s->clump_id, N * 4)) return fail(JDEM_ERR_CUDA, "upload: reading clump_id");

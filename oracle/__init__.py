@@ -60,7 +60,11 @@ def load_c(f64: bool = False) -> C.CDLL:
                           C.c_int, C.c_int, C.c_int]
         force.restype = C.c_int
         getattr(lib, "oracle_max_threads" + sfx).restype = C.c_int
+        contacts = getattr(lib, "oracle_contacts" + sfx)
+        contacts.argtypes = [C.c_int, C.c_int64, C.c_int, fp, fp, real, fp, fp, C.c_void_p, C.c_int64, C.c_int]
+        contacts.restype = C.c_int64
         lib.step, lib.force, lib.max_threads = step, force, getattr(lib, "oracle_max_threads" + sfx)
+        lib.contacts = contacts
         _LIBS[f64] = lib
     return _LIBS[f64]
 
@@ -121,6 +125,30 @@ def c_force(dim, pos, rad, *, domain, box, anchor, cell_size, search_range=1, yo
     if rc != 0:
         raise RuntimeError(f"oracle_force failed ({rc})")
     return out
+
+
+def c_contacts(dim, pos, rad, *, domain, box, anchor, cell_size, threads=0):
+    """Canonical contact set of the C restatement: ``(i < j)`` pairs with
+    ``d_sq < (r_i + r_j)^2`` (float32 arithmetic of ``periodic.py:74-79``), as an
+    ``(n_pairs, 2)`` int64 array sorted lexicographically."""
+    lib = load_c(False)
+    pos = np.ascontiguousarray(pos, np.float32)
+    rad = np.ascontiguousarray(rad, np.float32)
+    N = pos.shape[0]
+    box3, anc3 = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    box3[:dim] = box
+    anc3[:dim] = anchor
+    args = (dim, N, DOMAIN[domain], _p(box3), _p(anc3), float(cell_size), _p(pos), _p(rad))
+    n = lib.contacts(*args, None, 0, int(threads))
+    if n < 0:
+        raise RuntimeError("oracle_contacts: allocation failed")
+    pairs = np.zeros((max(n, 1), 2), np.int64)
+    n2 = lib.contacts(*args, pairs.ctypes.data, n, int(threads))
+    if n2 != n:
+        raise RuntimeError(f"oracle_contacts: count changed between passes ({n} vs {n2})")
+    pairs = pairs[:n]
+    order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+    return pairs[order]
 
 
 def max_threads() -> int:

@@ -199,18 +199,17 @@ static inline void hertz_pair(const Grid* G, const real* pi, const real* pj, rea
   for (int a = 0; a < d; ++a) f[a] = mag * (rij[a] * inv);
 }
 
-/* compute_force via the cell list in the reference's visiting order. */
-static void cell_list_force(const Grid* G, int64_t n, const real* pos, const real* rad,
-                            const int32_t* mat, const int64_t* hash, const int64_t* start,
-                            const int64_t* perm, real* force, int acc64) {
+/* Stencil cell hashes of position p (cell_list.py:66-96): periodic axes wrap
+ * by floor-mod, other axes mark out-of-grid cells -1, and for periodic grids
+ * with fewer than 2*sr+1 cells along some axis a repeated hash becomes -1
+ * (_dedup_stencil_hashes, cell_list.py:90-96).  Returns the stencil size M. */
+static int stencil_hashes(const Grid* G, const real* p, int64_t* nh) {
   int d = G->dim;
   int side = 2 * G->sr + 1;
   int M = d == 3 ? side * side * side : side * side;
-#pragma omp parallel for schedule(dynamic, 256)
-  for (int64_t i = 0; i < n; ++i) {
+  {
     int64_t c[3];
-    coords_of(G, pos + i * d, c);
-    int64_t nh[343];
+    coords_of(G, p, c);
     for (int m = 0; m < M; ++m) {
       int off[3];
       int rem = m;
@@ -246,6 +245,19 @@ static void cell_list_force(const Grid* G, int64_t n, const real* pos, const rea
             break;
           }
     }
+  }
+  return M;
+}
+
+/* compute_force via the cell list in the reference's visiting order. */
+static void cell_list_force(const Grid* G, int64_t n, const real* pos, const real* rad,
+                            const int32_t* mat, const int64_t* hash, const int64_t* start,
+                            const int64_t* perm, real* force, int acc64) {
+  int d = G->dim;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t nh[343];
+    const int M = stencil_hashes(G, pos + i * d, nh);
     double tot64[3] = {0, 0, 0};
     real tot[3] = {0, 0, 0};
     for (int m = 0; m < M; ++m) {
@@ -479,6 +491,92 @@ int FN(oracle_force)(int dim, int64_t n, int domain, const real* box, const real
   free(perm);
   free(start);
   return 0;
+}
+
+/* Canonical contact set: pairs (i < j) with d_sq < (r_i + r_j)^2, d the
+ * displacement of periodic.py:74-79 (d - box * round(d * inv_box)) summed
+ * left to right, enumerated through the cell list (only pairs within one
+ * stencil, as in the reference).  The reference has no contact-set API;
+ * utils/contacts.py:21-86 keeps the candidates whose spring force is nonzero,
+ * i.e. whose overlap is positive.  Called with pairs == NULL it returns the
+ * count; otherwise it writes at most cap pairs, grouped by i in ascending
+ * order (j in visiting order within a group), and returns the count.  A
+ * negative return is an allocation failure. */
+int64_t FN(oracle_contacts)(int dim, int64_t n, int domain, const real* box, const real* anchor,
+                            real cell_size, const real* pos, const real* rad, int64_t* pairs,
+                            int64_t cap, int n_threads) {
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  Grid G;
+  memset(&G, 0, sizeof(G));
+  G.dim = dim;
+  G.domain = domain;
+  G.cell_req = cell_size;
+  G.sr = 1;
+  for (int a = 0; a < dim; ++a) {
+    G.box[a] = box[a];
+    G.anchor[a] = anchor[a];
+    G.inv_box[a] = 1.0f / box[a];
+  }
+  grid_setup(&G);
+  int64_t* hash = (int64_t*)malloc(sizeof(int64_t) * (size_t)max_i64(n, 1));
+  int64_t* perm = (int64_t*)malloc(sizeof(int64_t) * (size_t)max_i64(n, 1));
+  int64_t* start = (int64_t*)malloc(sizeof(int64_t) * (size_t)(G.ncell + 1));
+  int64_t* cnt = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  if (!hash || !perm || !start || !cnt) {
+    free(hash);
+    free(perm);
+    free(start);
+    free(cnt);
+    return -1;
+  }
+  build_cells(&G, n, pos, hash, start, perm);
+  int64_t total = 0;
+  for (int pass = 0; pass < (pairs ? 2 : 1); ++pass) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t nh[27];
+      const int M = stencil_hashes(&G, pos + i * dim, nh);
+      int64_t c = 0, o = pass ? cnt[i] : 0;
+      for (int m = 0; m < M; ++m) {
+        int64_t h = nh[m];
+        if (h < 0) continue;
+        for (int64_t k = start[h]; k < start[h + 1]; ++k) {
+          int64_t j = perm[k];
+          if (j <= i) continue;
+          real dsq = 0.0f;
+          for (int a = 0; a < dim; ++a) {
+            real x = pos[i * dim + a] - pos[j * dim + a];
+            if (domain == DOM_PERIODIC) x = x - G.box[a] * R_RINT(x * G.inv_box[a]);
+            dsq = a == 0 ? x * x : dsq + x * x;
+          }
+          real R = rad[i] + rad[j];
+          if (dsq < R * R) {
+            if (pass && o + c < cap) {
+              pairs[2 * (o + c)] = i;
+              pairs[2 * (o + c) + 1] = j;
+            }
+            ++c;
+          }
+        }
+      }
+      if (!pass) cnt[i] = c;
+    }
+    if (!pass) {
+      /* exclusive prefix: cnt[i] becomes the first output row of i */
+      for (int64_t i = 0; i < n; ++i) {
+        int64_t c = cnt[i];
+        cnt[i] = total;
+        total += c;
+      }
+    }
+  }
+  free(hash);
+  free(perm);
+  free(start);
+  free(cnt);
+  return total;
 }
 
 int FN(oracle_max_threads)(void) {
