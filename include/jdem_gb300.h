@@ -267,6 +267,15 @@ int jdem_set_stream(JdemHandle* h, void* stream);
  * by the next jdem_sync / jdem_step / jdem_stats. */
 int jdem_download_device_async(JdemHandle* h, JdemHostState* dev);
 
+/* Fault-path control of the many-step kernel's grid barrier (graph_mode 0, small
+ * systems): a barrier polls at most `spins` times (0: the default, about a second)
+ * before it gives up, and with extra_arrivals > 0 it also waits for that many
+ * arrivals that never come, so every barrier gives up.  A barrier that gave up makes
+ * the next jdem_sync / jdem_step return JDEM_ERR_TIMEOUT; the steps of that chunk are
+ * incomplete and the handle runs later steps one launch per step.  For tests of the
+ * timeout path; normal use never calls it. */
+int jdem_set_barrier_limit(JdemHandle* h, uint32_t spins, uint32_t extra_arrivals);
+
 /* Contact forces of one sphere system from caller-owned device buffers, without
  * allocating device memory.  No counterpart in the reference: it exists for callers
  * that may not call cudaMalloc while they run, such as an XLA FFI handler (XLA owns

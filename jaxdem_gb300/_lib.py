@@ -160,6 +160,7 @@ _PROTOS = [
     ("jdem_stream", [C.c_void_p], C.c_void_p),
     ("jdem_set_stream", [C.c_void_p, C.c_void_p], C.c_int),
     ("jdem_shape", [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
+    ("jdem_set_barrier_limit", [C.c_void_p, C.c_uint32, C.c_uint32], C.c_int),
     ("jdem_download_device_async", [C.c_void_p, C.POINTER(HostState)], C.c_int),
     ("jdem_host_register", [C.c_void_p, C.c_size_t], C.c_int),
     ("jdem_host_unregister", [C.c_void_p], C.c_int),
@@ -446,6 +447,10 @@ class Engine:
 
     def stream(self) -> int:
         return int(self.lib.jdem_stream(self.h) or 0)
+
+    def set_barrier_limit(self, spins: int, extra_arrivals: int = 0) -> None:
+        """Fault-path control of the many-step grid barrier (tests of the timeout path)."""
+        self._check(self.lib.jdem_set_barrier_limit(self.h, int(spins), int(extra_arrivals)))
 
     def set_stream(self, stream: int) -> None:
         """Queue later work on ``stream`` (a ``cudaStream_t`` as an int, e.g.

@@ -985,7 +985,9 @@ int JdemHandle::sync_status() {
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.ctl, h_status, sizeof(Ctl), cudaMemcpyHostToDevice, stream));
     JDEM_CUDA_TRY(this, cudaStreamSynchronize(stream));
     sticky_status &= ~(unsigned int)ST_BARRIER_TIMEOUT;
-    return fail(JDEM_ERR_CUDA, "many-step kernel: a grid barrier timed out; the steps of that chunk are incomplete");
+    return fail(JDEM_ERR_TIMEOUT,
+                "many-step kernel: a grid barrier timed out; the steps of that chunk are incomplete "
+                "(later steps run one launch per step)");
   }
 
   return JDEM_OK;
@@ -1304,6 +1306,15 @@ int jdem_stats(JdemHandle* h, JdemStats* out) {
 }
 
 void* jdem_stream(JdemHandle* h) { return h ? (void*)h->stream : nullptr; }
+
+int jdem_set_barrier_limit(JdemHandle* h, uint32_t spins, uint32_t extra_arrivals) {
+  if (!h) return JDEM_ERR_BAD_ARG;
+  h->b.bar_spins = spins;
+  h->b.bar_extra = extra_arrivals;
+  h->drop_graphs();  // captured kernel parameters hold the old values
+  if (extra_arrivals == 0) h->use_multi = true;
+  return JDEM_OK;
+}
 
 int jdem_shape(const JdemHandle* h, int64_t* n_particles, int32_t* dim) {
   if (!h || !n_particles || !dim) return JDEM_ERR_BAD_ARG;

@@ -48,10 +48,13 @@ __device__ __forceinline__ float4 ldc4(const float4* p) { return __ldcg(p); }
 // into ctl->mx[s % 3] and arrives with one release add on the never-reset
 // arrival count; every block then polls the count until it reaches its
 // target (the launch's base plus gridDim.x per barrier), takes an acquire
-// fence and reads the slot.  Bounded: a block that polls kBarrierSpins times
-// records ST_BARRIER_TIMEOUT and returns false.
+// fence and reads the slot.  Bounded: a block that polls max_spins times
+// records ST_BARRIER_TIMEOUT and returns false.  `extra` arrivals beyond the
+// grid's are awaited too; they never come, so extra > 0 makes every block
+// give up (the timeout path, exercised by a test through jdem_set_barrier_limit).
 __device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& target, unsigned int s,
-                                                 const float* s_wmax, float& m2) {
+                                                 const float* s_wmax, float& m2, unsigned int max_spins,
+                                                 unsigned int extra) {
   __shared__ int s_ok;
   __shared__ unsigned int s_m2;
   __syncthreads();
@@ -65,8 +68,8 @@ __device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& target,
     target += gridDim.x;
     int ok = 1;
     unsigned int spins = 0;
-    while ((int)(ld_relaxed_u32(&ctl->bar_count) - target) < 0) {
-      if (++spins > kBarrierSpins) {
+    while ((int)(ld_relaxed_u32(&ctl->bar_count) - (target + extra)) < 0) {
+      if (++spins > max_spins) {
         atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
         ok = 0;
         break;
@@ -211,7 +214,7 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
     d2 = warp_max(d2);
     if (lane == 0) s_wmax[threadIdx.x >> 5] = d2;
     float m2;
-    ok = grid_barrier_max(ctl, target, s, s_wmax, m2);
+    ok = grid_barrier_max(ctl, target, s, s_wmax, m2, b.bar_spins ? b.bar_spins : kBarrierSpins, b.bar_extra);
     if (!ok) break;
     // k_fin: bound += sqrt(max squared drift); positions flip
     bound = bound + sqrtf(m2);

@@ -24,7 +24,19 @@
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress and caches it (the
 // host-side symbol is only a stand-in and must never be passed to a kernel).
-// Make that first call before any stream capture.
+// Make that first call before any stream capture.  The cache is keyed on the
+// device's current context: after cudaDeviceReset (a new primary context, the
+// module loaded again, possibly elsewhere) the next call looks the address up
+// again, and that call too must come before any stream capture.
+//
+// Order inside a cell is ascending particle index, so the forces are the same
+// bit for bit from call to call: cells of at most kSmallCell particles are
+// insertion-sorted by one thread; larger cells (the coarsened grids of dilute
+// or clustered inputs) are ordered by a block that marks the members in a
+// bitmap of all particle indices and writes the marked indices out in order,
+// O(n / 32 + m) per cell instead of O(m^2).
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -37,6 +49,11 @@ namespace {
 
 constexpr int kMaxP = JDEM_NOALLOC_MAX_PARTICLES;
 constexpr int kMaxC = JDEM_NOALLOC_MAX_CELLS;
+constexpr int kSmallCell = 32;                          // insertion sort up to this many members
+constexpr int kMaxLarge = kMaxP / (kSmallCell + 1) + 1; // cells with more members, at most
+constexpr int kBitWords = (kMaxP + 31) / 32;            // bitmap of every particle index
+constexpr int kSortThreads = 1024;
+static_assert(kBitWords % kSortThreads == 0, "bitmap words split evenly over the sort block");
 
 struct NaParams {
   float box[3];
@@ -59,6 +76,8 @@ struct NoAllocScratch {
   int key[kMaxP];
   int slot[kMaxP];
   int perm[kMaxP];
+  int n_large;            // cells with more than kSmallCell members (zeroed by k_na_setup)
+  int large[kMaxLarge];   // their indices
 };
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
@@ -130,6 +149,7 @@ __global__ void k_na_setup(NoAllocScratch* S, int n, int dim, int domain, float 
     P.domain = domain;
     P.n = n;
     P.k = k;
+    S->n_large = 0;
   }
   for (int c = threadIdx.x; c < kMaxC; c += blockDim.x) S->cnt[c] = 0;
 }
@@ -184,11 +204,16 @@ __global__ void k_na_scatter(NoAllocScratch* S) {
   S->perm[S->start[S->key[i]] + S->slot[i]] = i;
 }
 
-// Ascending index inside each cell: a deterministic visiting order.
+// Ascending index inside each cell: a deterministic visiting order.  Small
+// cells are insertion-sorted here; larger ones are listed for k_na_bigsort.
 __global__ void k_na_cellsort(NoAllocScratch* S) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S->prm.ncell) return;
   int a = S->start[c], e = S->start[c + 1];
+  if (e - a > kSmallCell) {
+    S->large[atomicAdd(&S->n_large, 1)] = c;  // at most n / (kSmallCell + 1) cells
+    return;
+  }
   for (int i = a + 1; i < e; ++i) {
     int x = S->perm[i];
     int j = i - 1;
@@ -197,6 +222,54 @@ __global__ void k_na_cellsort(NoAllocScratch* S) {
       --j;
     }
     S->perm[j + 1] = x;
+  }
+}
+
+// A cell of m > kSmallCell members in ascending index order: the members set
+// their bits in a shared bitmap of all n indices, then a block scan of the
+// words' bit counts gives each word its first output position, and each
+// thread writes its words' set bits out in increasing order.
+__global__ void __launch_bounds__(kSortThreads) k_na_bigsort(NoAllocScratch* S) {
+  __shared__ unsigned int bm[kBitWords];
+  __shared__ int part[kSortThreads];
+  constexpr int kPer = kBitWords / kSortThreads;  // words per thread
+  const int words = (S->prm.n + 31) / 32;
+  const int n_large = S->n_large;
+  for (int L = blockIdx.x; L < n_large; L += gridDim.x) {
+    const int c = S->large[L];
+    const int a = S->start[c], e = S->start[c + 1];
+    for (int w = threadIdx.x; w < words; w += kSortThreads) bm[w] = 0u;
+    __syncthreads();
+    for (int k = a + threadIdx.x; k < e; k += kSortThreads) {
+      const int i = S->perm[k];
+      atomicOr(&bm[i >> 5], 1u << (i & 31));
+    }
+    __syncthreads();
+    // thread t owns words [t * kPer, (t + 1) * kPer)
+    const int w0 = threadIdx.x * kPer;
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) cnt += w0 + q < words ? __popc(bm[w0 + q]) : 0;
+    part[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = 1; o < kSortThreads; o <<= 1) {
+      const int v = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += v;
+      __syncthreads();
+    }
+    int out = a + part[threadIdx.x] - cnt;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      if (w0 + q >= words) break;
+      unsigned int bits = bm[w0 + q];
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        S->perm[out++] = (w0 + q) * 32 + b;
+        bits &= bits - 1u;
+      }
+    }
+    __syncthreads();  // the bitmap and the scan are reused by the next cell
   }
 }
 
@@ -254,14 +327,53 @@ __global__ void k_na_force(NoAllocScratch* S, const float* __restrict__ pos, con
 }
 
 std::mutex g_mtx;
-NoAllocScratch* g_dev_ptr[256] = {nullptr};
+// per device: the context the address was looked up in, and the address
+struct DevScratch {
+  unsigned long long ctx_id = 0;
+  NoAllocScratch* ptr = nullptr;
+};
+DevScratch g_dev[256];
+
+// Unique id of the calling thread's current context (never reused within the
+// process, unlike a context's address), through the driver entry points the
+// runtime exposes; 0 when unavailable.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      get_current = (GetCurrent)f1;
+      get_id = (GetId)f2;
+    }
+    cudaGetLastError();
+    looked_up = true;
+  }
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 }  // namespace
 
 extern "C" int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain, const float* box_size,
                                           const float* anchor, float young, const float* pos, const float* rad,
                                           float* force, void* stream) {
-  if (n < 0 || n > kMaxP) {
+  if (n < 0) {
+    std::fprintf(stderr, "jdem_compute_force_noalloc: n = %lld is negative\n", (long long)n);
+    return JDEM_ERR_BAD_ARG;
+  }
+  if (n > kMaxP) {
     std::fprintf(stderr,
                  "jdem_compute_force_noalloc: n = %lld exceeds the fixed scratch limit of %d particles "
                  "(JDEM_NOALLOC_MAX_PARTICLES); use jdem_create/jdem_compute_force for larger systems\n",
@@ -278,17 +390,23 @@ extern "C" int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain
   NoAllocScratch* S = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mtx);
-    if (!g_dev_ptr[dev]) {
+    // first call on this device, or a new context since (cudaDeviceReset):
+    // look the array's address up in the current context
+    const unsigned long long ctx = current_context_id();
+    DevScratch& d = g_dev[dev];
+    if (!d.ptr || ctx != d.ctx_id) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) {
+        cudaGetLastError();
         std::fprintf(stderr, "jdem_compute_force_noalloc: cudaGetSymbolAddress failed: %s\n",
                      cudaGetErrorString(e));
         return JDEM_ERR_CUDA;
       }
-      g_dev_ptr[dev] = (NoAllocScratch*)p;
+      d.ptr = (NoAllocScratch*)p;
+      d.ctx_id = ctx;
     }
-    S = g_dev_ptr[dev];
+    S = d.ptr;
   }
   cudaStream_t st = (cudaStream_t)stream;
   float b[3] = {1, 1, 1}, an[3] = {0, 0, 0};
@@ -303,6 +421,7 @@ extern "C" int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain
   k_na_scan<<<1, 1024, 0, st>>>(S);
   k_na_scatter<<<pb, 256, 0, st>>>(S);
   k_na_cellsort<<<(kMaxC + 255) / 256, 256, 0, st>>>(S);
+  k_na_bigsort<<<64, kSortThreads, 0, st>>>(S);
   if (dim == 3) k_na_force<3><<<pb, 256, 0, st>>>(S, pos, rad, force);
   else k_na_force<2><<<pb, 256, 0, st>>>(S, pos, rad, force);
   cudaError_t e = cudaGetLastError();

@@ -84,6 +84,61 @@ def test_noalloc_matches_regular_entry_point_twice_in_a_row():
         assert err <= 1e-5, f"{w.name}: noalloc vs jdem_compute_force err {err}"
 
 
+MAX_CELLS = 131072
+
+
+def _check(w):
+    got = _noalloc_force(w)
+    ref = _regular_force(w)
+    assert np.isfinite(got).all()
+    err = force_err(got, ref)
+    assert err <= 1e-5, f"{w.name}: noalloc vs jdem_compute_force err {err}"
+    return got
+
+
+def test_noalloc_free_domain():
+    """Free domain: the grid's origin and extent come from the device bounding box."""
+    rng = np.random.Generator(np.random.PCG64(23))
+    w = W.periodic_system("free", rng, 4000, 3, rng.choice([0.5, 0.7], size=4000), 0.4, 0.1, 1e-3, 1)
+    w.domain = "free"
+    w.pos = (w.pos - 37.5).astype(F32)  # away from the origin: the bounding box sets the frame
+    _check(w)
+
+
+def test_noalloc_coarsens_a_dilute_grid():
+    """A dilute periodic box whose grid at 2 r_max has far more than 131072 cells: the
+    device coarsens the grid until it fits the fixed scratch, and the forces still match."""
+    rng = np.random.Generator(np.random.PCG64(24))
+    N = 30000
+    w = W.periodic_system("dilute", rng, N, 3, np.full(N, 0.5), 0.004, 0.1, 1e-3, 1)
+    # make some contacts: pairs of overlapping spheres
+    w.pos[1::2] = (w.pos[0::2] + rng.uniform(-0.5, 0.5, size=w.pos[0::2].shape)).astype(F32)
+    L = float(w.box_size[0])
+    uncoarsened = int(np.floor(L / (2 * float(w.rad.max())))) ** 3
+    assert uncoarsened > 10 * MAX_CELLS, "the input must need coarsening"
+    got = _check(w)
+    assert np.abs(got).max() > 1.0, "the case should have contacts"
+
+
+def test_noalloc_clustered_cells_keep_a_deterministic_order():
+    """A free-domain cluster with one far-away sphere: the coarsened grid puts thousands of
+    spheres in one cell, which takes the bitmap ordering path.  Two calls give identical
+    forces bit for bit, and both match the regular entry point."""
+    rng = np.random.Generator(np.random.PCG64(25))
+    N = 12000
+    w = W.periodic_system("cluster", rng, N, 3, rng.choice([0.5, 0.7], size=N), 0.5, 0.1, 1e-3, 1)
+    w.domain = "free"
+    w.pos[-1] = np.array([5.0e3, -4.0e3, 3.0e3], F32)
+    a = _check(w)
+    b = _noalloc_force(w)
+    assert np.array_equal(a, b)
+
+
 def test_noalloc_rejects_oversized_input():
     rc = _fn()(3, MAX_P + 1, 1, None, None, 1.0, None, None, None, None)
     assert rc == 2  # JDEM_ERR_CAPACITY_OVERFLOW, before any device work
+
+
+def test_noalloc_rejects_negative_n():
+    rc = _fn()(3, -5, 1, None, None, 1.0, None, None, None, None)
+    assert rc == 1  # JDEM_ERR_BAD_ARG
