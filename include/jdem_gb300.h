@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 6
+#define JDEM_ABI_VERSION 7
 
 enum {
   JDEM_OK = 0,
@@ -103,6 +103,12 @@ typedef struct {
   int32_t force_law;            /* JDEM_FORCE_* */
   const float* material_props;  /* Cundall-Strack only: M*4 per material (young, shear modulus
                                    young / (2 (1 + poisson)), mu, mu_r) */
+  float prune_skin;             /* dynamic pruning of the Verlet list (systems above 32768 slots,
+                                   spring / Hertz spheres): on steps between re-sorts the force
+                                   kernel walks an inner list of the pairs within
+                                   r_i + r_j + prune_skin, rebuilt from the full list whenever
+                                   the drift since its build exceeds prune_skin / 2.
+                                   0: skin / 3; < 0: off (every step walks the full list) */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is
@@ -144,7 +150,7 @@ typedef struct {
   int32_t list_capacity;     /* entries per Verlet-list row (0: no list) */
   int32_t list_tiles;        /* cell bricks of the shared-memory list path (0: slot-order path) */
   int32_t many_step;         /* 1: step chunks run as one cooperative launch of many steps (small systems) */
-  int32_t reserved;
+  int32_t prunes;            /* inner-list builds of the dynamic pruning since the last upload */
 } JdemStats;
 
 /* ABI version of the loaded library (JDEM_ABI_VERSION). */

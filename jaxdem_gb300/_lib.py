@@ -76,6 +76,7 @@ class Config(C.Structure):
         ("graph_mode", C.c_int32),
         ("force_law", C.c_int32),
         ("material_props", C.POINTER(C.c_float)),
+        ("prune_skin", C.c_float),
     ]
 
 
@@ -128,7 +129,7 @@ class Stats(C.Structure):
         ("list_capacity", C.c_int32),
         ("list_tiles", C.c_int32),
         ("many_step", C.c_int32),
-        ("reserved", C.c_int32),
+        ("prunes", C.c_int32),
     ]
 
 
@@ -205,7 +206,7 @@ class Engine:
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
                  device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring",
-                 material_props: Optional[np.ndarray] = None):
+                 material_props: Optional[np.ndarray] = None, prune_skin: float = 0.0):
         """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k,
         (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``), or the damping ratio
         beta for ``"cundallstrack"``, which also takes ``material_props`` (M, 4)
@@ -256,6 +257,8 @@ class Engine:
         if force_law not in FORCE_LAW:
             raise ValueError(f"force_law must be one of {sorted(FORCE_LAW)}")
         cfg.force_law = FORCE_LAW[force_law]
+        # inner-list margin of the dynamic pruning (0: skin / 3, < 0: off)
+        cfg.prune_skin = float(prune_skin)
         self.force_law = force_law
         self._props = None
         if material_props is not None:

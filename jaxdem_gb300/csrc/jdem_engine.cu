@@ -153,12 +153,14 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   graph_mode = cfg->graph_mode;
   use_conditional = graph_mode == 0;
   nl_request = cfg->neighbor_list;
+  if (!std::isfinite(cfg->prune_skin)) return fail(JDEM_ERR_BAD_ARG, "config: prune_skin must be finite");
+  prune_req = cfg->prune_skin;
   int rc0 = set_systems(cfg->systems, S);
   if (rc0) return rc0;
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   stream = own;
-  JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, 64));
+  JDEM_CUDA_TRY(this, cudaMallocHost((void**)&h_status, sizeof(Ctl)));
   int rc;
   if ((rc = dalloc((void**)&b.ctl, sizeof(Ctl)))) return rc;
   if ((rc = dalloc((void**)&d_young, sizeof(float) * n_mat * n_mat))) return rc;
@@ -500,8 +502,12 @@ int JdemHandle::plan_list(int cap) {
   drop_graphs();
   dfree(b.nbr);
   dfree(b.ncnt);
+  dfree(b.nbr2);
+  dfree(b.ncnt2);
   b.nbr = nullptr;
   b.ncnt = nullptr;
+  b.nbr2 = nullptr;
+  b.ncnt2 = nullptr;
   b.nl_cap = 0;
   nl_alloc_ints = 0;
   b.nl_skin = skin;
@@ -509,6 +515,14 @@ int JdemHandle::plan_list(int cap) {
   int rc;
   if ((rc = dalloc((void**)&b.nbr, sizeof(int32_t) * (size_t)need))) return rc;
   if ((rc = dalloc((void**)&b.ncnt, sizeof(int32_t) * (size_t)P))) return rc;
+  // dynamic pruning: the fused kernel of large sphere systems (k_force) only
+  const float ps = prune_req == 0.0f ? skin / 3.0f : prune_req;
+  b.prune_skin = 0.0f;
+  if (ps > 0.0f && ps < skin && P > kSmallForceSlots && b.law != LAW_CS && b.NC == 0) {
+    if ((rc = dalloc((void**)&b.nbr2, sizeof(int32_t) * (size_t)need))) return rc;
+    if ((rc = dalloc((void**)&b.ncnt2, sizeof(int32_t) * (size_t)P))) return rc;
+    b.prune_skin = ps;
+  }
   // empty rows until the first build
   JDEM_CUDA_TRY(this, cudaMemsetAsync(b.ncnt, 0, sizeof(int32_t) * (size_t)P, stream));
   dfree(b.posw);
@@ -528,6 +542,8 @@ int JdemHandle::reset_ctl() {
   std::memset(&c, 0, sizeof(c));
   c.need_rebuild = 1u;
   c.skin_half = 0.5f * skin;
+  c.prune = 1u;
+  c.pskin_half = b.nbr2 ? 0.5f * b.prune_skin : 0.0f;
   JDEM_CUDA_TRY(this, cudaMemcpyAsync(b.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, stream));
   return JDEM_OK;
 }
@@ -936,6 +952,7 @@ int JdemHandle::sync_status() {
   const Ctl* c = (const Ctl*)h_status;
   sticky_status |= c->status & ~(unsigned int)ST_NL_OVERFLOW;
   rebuilds = c->rebuilds;
+  prunes = c->prunes;
   if (c->status & ST_NL_OVERFLOW) {
     // a list row overflowed: those steps used the cell traversal (still
     // exact); double the capacity and rebuild the list before the next step
@@ -1301,7 +1318,7 @@ int jdem_stats(JdemHandle* h, JdemStats* out) {
   out->list_capacity = h->b.nl_cap;
   out->list_tiles = h->b.n_tiles;
   out->many_step = h->multi_used ? 1 : 0;
-  out->reserved = 0;
+  out->prunes = (int32_t)h->prunes;
   return JDEM_OK;
 }
 

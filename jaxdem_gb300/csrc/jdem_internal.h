@@ -70,6 +70,7 @@ struct JdemHandle {
   bool any_free = false;
   bool use_nl = true;
   int nl_request = 0;
+  float prune_req = 0.0f;  // JdemConfig.prune_skin (0: skin / 3, < 0: off)
   bool rot_active = false;
   bool uploaded = false;
   bool bbox_pending = false;
@@ -114,6 +115,7 @@ struct JdemHandle {
   long long device_bytes = 0;
   long long steps_done = 0;
   long long rebuilds = 0;
+  long long prunes = 0;  // inner-list builds (dynamic pruning) since the upload
   long long nl_regrowths = 0;
   unsigned int sticky_status = 0;
   std::string err;

@@ -28,12 +28,21 @@ enum : int { FIN_AFTER_FORCE = 1, FIN_SET_COND = 2 };
 
 __global__ void k_fin(Ctl* ctl, int flags, cudaGraphConditionalHandle h) {
   float m2 = __uint_as_float(atomicExch(&ctl->maxdisp2, 0u));
-  float bd = ctl->bound + sqrtf(m2);
+  const float d = sqrtf(m2);
+  float bd = ctl->bound + d;
   ctl->bound = bd;
   unsigned int nr = ctl->need_rebuild;
   if (bd > ctl->skin_half) nr = 1u;
   ctl->need_rebuild = nr;
   unsigned int nd = ctl->nl_dirty;
+  // dynamic pruning: a force pass that rebuilt the inner list (prune or a
+  // fresh outer list) restarts the drift count from its positions; the next
+  // force pass prunes once the drift exceeds half the prune skin
+  const bool pruned = (flags & FIN_AFTER_FORCE) && (ctl->prune | nd);
+  if (pruned && ctl->pskin_half > 0.0f) ctl->prunes += 1u;
+  const float pb = pruned ? d : ctl->pbound + d;
+  ctl->pbound = pb;
+  ctl->prune = pb > ctl->pskin_half ? 1u : 0u;
   if (flags & FIN_AFTER_FORCE) {
     ctl->pos_sel ^= 1u;
     nd = 0u;
@@ -532,16 +541,23 @@ __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
   const bool use_list = NL && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  // dynamic pruning (uniform over the launch): a prune pass walks the full
+  // list and writes the inner one; the other passes walk the inner list
+  const bool pruning = use_list && b.nbr2 != nullptr;
+  const bool prune = pruning && (ld_cg_u32(&b.ctl->prune) | ld_cg_u32(&b.ctl->nl_dirty)) != 0u;
   float d2max = 0.0f;
   if (t < b.P) {
-    const int n = use_list ? b.ncnt[t] : 0;
-    const int32_t* nb = use_list ? b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31) : nullptr;
+    const long long row = ((t >> 5) * b.nl_cap) * 32 + (t & 31);
+    const bool inner = pruning && !prune;
+    const int n = use_list ? (inner ? b.ncnt2[t] : b.ncnt[t]) : 0;
+    const int32_t* nb = use_list ? (inner ? b.nbr2 : b.nbr) + row : nullptr;
     if (use_list) {
-      prefetch_list_block(b, t, n);
+      prefetch_list_block(b, t, n, inner);
       // the velocity record, read after the contact loop
       asm volatile("prefetch.global.L2 [%0];" ::"l"(&b.vel[sel][t]));
     }
-    d2max = particle_step<DIM, GENERAL, LAW>(b, mode, t, sel, ps, use_list, nb, n, 32);
+    d2max = particle_step<DIM, GENERAL, LAW>(b, mode, t, sel, ps, use_list, nb, n, 32,
+                                             prune ? b.nbr2 + row : nullptr, prune ? b.ncnt2 + t : nullptr);
   }
   if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
 }

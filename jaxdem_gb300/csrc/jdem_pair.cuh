@@ -106,8 +106,9 @@ struct ContactSum {
   // the material and bond lookups of GENERAL; self pairs are never passed.
   // may_wrap == false asserts d - box * round(d / box) == d on every axis (a
   // list entry of the same periodic image), so the minimum image is skipped.
-  __device__ __forceinline__ void add(const Bufs& b, unsigned int sel, int j, const float4& pj,
-                                      bool may_wrap = true) {
+  // Returns the squared distance (the pruning test of k_force reads it).
+  __device__ __forceinline__ float add(const Bufs& b, unsigned int sel, int j, const float4& pj,
+                                       bool may_wrap = true) {
     float dx, dy, dz;
     const float dsq = pair_disp<DIM>(*sp, per && may_wrap, pi, pj, dx, dy, dz);
     const float R = pi.w + pj.w;
@@ -123,12 +124,13 @@ struct ContactSum {
         int oj = b.orig[sel][j];
         bool bonded = false;
         for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[(long long)oi * b.bond_w + w] == oj);
-        if (bonded) return;
+        if (bonded) return dsq;
       }
       // spheres of one rigid clump do not interact (clump_i != clump_j)
-      if (GENERAL && b.sclump && b.sclump[b.orig[sel][j]] == ci) return;
+      if (GENERAL && b.sclump && b.sclump[b.orig[sel][j]] == ci) return dsq;
       contact(k, dsq, R, pj.w, dx, dy, dz);
     }
+    return dsq;
   }
 
   // Contact force of one candidate, summed with the two-sum accumulator.
@@ -230,17 +232,41 @@ __device__ __forceinline__ float integrate_particle(const Bufs& b, int mode, lon
 // One particle (slot t) of the fused step: contact force from the Verlet list
 // `nb` (n slot indices, `stride` ints apart) when use_list is set, else from
 // the stencil cells (periodic minimum image of periodic.py:74-79), then
-// integrate_particle.
+// integrate_particle.  With `prune_out` set (a prune pass of the dynamic
+// pruning) the entries within r_i + r_j + b.prune_skin are also copied, in
+// list order, to the inner row prune_out (same stride) and their count to
+// *prune_cnt.
 template <int DIM, bool GENERAL, int LAW>
 __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long long t, unsigned int sel,
                                                unsigned int ps, bool use_list, const int32_t* __restrict__ nb,
-                                               int n, int stride) {
+                                               int n, int stride, int32_t* __restrict__ prune_out = nullptr,
+                                               int32_t* __restrict__ prune_cnt = nullptr) {
   const float4* __restrict__ P = b.pos[ps];
   const float4 pi = P[t];
   const uint32_t tg = b.tag[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
   ContactSum<DIM, GENERAL, LAW> acc(b, sp, pi, tg, sel, t);
-  if (use_list) {
+  if (use_list && prune_out) {
+    // prune pass: the full row, keeping the entries the next passes need
+    int m = 0;
+    for (int k = 0; k < n; k += 4) {
+      uint32_t e[4];
+      float4 q[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[u] = k + u < n ? (uint32_t)__ldcs(&nb[(k + u) * stride]) : 0u;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (k + u < n) {
+          const float dsq = acc.add(b, sel, (int)(e[u] & kEntrySlot), q[u], GENERAL || (e[u] & kEntryImage) != 0u);
+          const float rc = (pi.w + q[u].w + b.prune_skin) * 1.0001f;
+          if (dsq < rc * rc) prune_out[(m++) * stride] = (int32_t)e[u];
+        }
+      }
+    }
+    *prune_cnt = m;
+  } else if (use_list) {
     for (int k = 0; k < n; k += 4) {
       uint32_t e[4];
       float4 q[4];

@@ -50,3 +50,47 @@ def osystem(w, domain=None, cell_size=None, search_range=None, young=None, linea
 
 def ostate(w, **kw):
     return R.make_state(w.pos, vel=w.vel, rad=w.rad, mass=w.mass, **kw)
+
+
+# ---------------------------------------------------------------- golden vectors of the reference
+# tests/golden/reference_<case>.npz hold inputs and outputs of JaxDEM's own State/System code
+# (tests/golden/make_reference_golden.py); these helpers turn a case into oracle objects.
+
+def load_reference_case(name, x64=False):
+    import json
+    from pathlib import Path
+
+    p = Path(__file__).resolve().parent / "golden" / f"reference_{name}{'_x64' if x64 else ''}.npz"
+    z = np.load(p)
+    d = {k: z[k] for k in z.files}
+    d["meta"] = json.loads(str(d["meta"]))
+    return d
+
+
+def reference_case_names():
+    from pathlib import Path
+
+    g = Path(__file__).resolve().parent / "golden"
+    return sorted(p.stem[len("reference_"):] for p in g.glob("reference_*.npz") if not p.stem.endswith("_x64"))
+
+
+def reference_osystem(d, dtype=np.float32):
+    """The oracle's System for a golden case (the reference's cell list, laws and integrators)."""
+    m = d["meta"]
+    dim = m["dim"]
+    _, mask = R.cell_list_create(d["rad"], dim)
+    law = m.get("law", "spring")
+    young = np.asarray(d["young_eff"], dtype)
+    if law == "hertz":
+        young = R.hertz_constant(np.asarray(m.get("young", [1.0e3])), np.full(len(m.get("young", [1.0e3])), 0.3))
+    grav = np.zeros(dim, dtype) if not m.get("gravity") else np.asarray(m["gravity"], dtype)
+    return R.OSystem(dim=dim, domain=m["domain"], box_size=np.asarray(d["box"], dtype).copy(),
+                     anchor=np.asarray(d["anchor"], dtype).copy(), young_eff=np.asarray(young, dtype),
+                     dt=dtype(m["dt"]), cell_size=dtype(d["cell_size"]), neighbor_mask=mask, gravity=grav,
+                     restitution=dtype(m.get("restitution", 1.0)), linear=m.get("linear", "verlet"),
+                     rotation=m.get("rotation", "verletspiral"), force_law=law)
+
+
+def reference_ostate(d, dtype=np.float32):
+    return R.make_state(d["pos"], vel=d["vel"], rad=d["rad"], mass=d["mass"], mat_id=d["mat_id"],
+                        ang_vel=d["ang_vel"], inertia=d["inertia"], dtype=dtype)
