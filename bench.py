@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--graph-mode", type=int, default=0, choices=[0, 1, 2],
                    help="0 conditional re-sort nodes, 1 plain graphs (profilers see every kernel), 2 no graphs")
     p.add_argument("--skin", type=float, default=None)
+    p.add_argument("--prune-skin", type=float, default=0.0,
+                   help="inner-list margin of the Verlet-list dynamic pruning (0: skin / 3, < 0: off)")
     p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -227,13 +229,15 @@ def run_ours(args, rank, world, dist):
         skin = autotune.default_skin(rmax)
     else:
         def mk(sk):
-            return Engine(w.dim, [w.desc()], young, skin=sk, chunk_steps=CHUNK, device=dev)
+            return Engine(w.dim, [w.desc()], young, skin=sk, chunk_steps=CHUNK, device=dev,
+                          prune_skin=args.prune_skin)
 
         skin, timings = autotune.tune_skin(mk, lambda e: e.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel),
                                            rmax, key=autotune.workload_key(w))
         tuning = {"skin_over_rmax": round(skin / rmax, 3),
                   "ms_per_step_by_skin": {str(k): round(v * 1e3, 4) for k, v in timings.items()}}
-    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev, graph_mode=args.graph_mode)
+    eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev, graph_mode=args.graph_mode,
+                 prune_skin=args.prune_skin)
     eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -250,7 +254,8 @@ def run_ours(args, rank, world, dist):
         eng.step(c)
     graphs_before = eng.stats()["graphs"]
     torch.cuda.synchronize()
-    rebuilds_before = eng.stats()["rebuilds"]
+    st0 = eng.stats()
+    rebuilds_before, prunes_before = st0["rebuilds"], st0["prunes"]
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler(dev)
@@ -310,7 +315,8 @@ def run_ours(args, rank, world, dist):
         outb = {"pos_c": np.empty_like(w.pos), "vel": np.empty_like(w.vel), "force": np.empty_like(w.pos)}
         for a in list(host.values()) + list(outb.values()):
             host_register(a)
-        e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev)
+        e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev,
+                         prune_skin=args.prune_skin)
         e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
         e2e_eng.step(K)  # the timed call sequence once: every graph it launches is captured here
         e2e_graphs = e2e_eng.stats()["graphs"]
@@ -356,6 +362,8 @@ def run_ours(args, rank, world, dist):
                    "parallelism": "replicas" if world > 1 else "single",
                    "resorts_in_timed_region": rebuilds_timed,
                    "graphs_captured_in_timed_region": graphs_captured_timed,
+                   "prune_skin": "off" if args.prune_skin < 0 else (args.prune_skin or skin / 3.0),
+                   "prunes_in_timed_region": stats["prunes"] - prunes_before,
                    "verlet_list": {"capacity": stats["list_capacity"], "tiles": stats["list_tiles"],
                                    "regrowths": stats["list_regrowths"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
