@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 7
+#define JDEM_ABI_VERSION 8
 
 enum {
   JDEM_OK = 0,
@@ -307,7 +307,9 @@ int jdem_compute_force_noalloc(int32_t dim, int64_t n, int32_t domain, const flo
  * requests together (one batched launch per kernel) by
  * min(chunk_steps, smallest remaining count).  Between epochs a request's
  * state stays on the device (repacked device-to-device when the active set
- * changes).  Spheres only, one material; rotation integrators are not run. */
+ * changes).  Spheres with the spring or Hertz law and the server's material
+ * table; each request brings its own domain, integrators (rotation included),
+ * dt, material ids and rotational state. */
 typedef struct JdemServer JdemServer;
 
 typedef struct {
@@ -318,7 +320,10 @@ typedef struct {
   int64_t target_particles;  /* admit while the active particles stay below this (<= 0: 4 Mi) */
   double hbm_budget_bytes;   /* admission limit on the resident footprint (<= 0: 150e9) */
   float skin;                /* binning skin of the batch */
-  float young;               /* spring stiffness */
+  float young;               /* spring stiffness when n_materials is 0 */
+  int32_t force_law;         /* JDEM_FORCE_SPRING or JDEM_FORCE_HERTZ (System.force_model) */
+  int32_t n_materials;       /* size M of young_eff (0: one material of stiffness `young`) */
+  const float* young_eff;    /* M*M pair constants, as JdemConfig.young_eff (copied at create) */
 } JdemServeConfig;
 
 typedef struct {
@@ -328,6 +333,9 @@ typedef struct {
   const float* vel;
   const float* rad;
   const float* mass;
+  const int32_t* mat_id;     /* (n) material ids, NULL: material 0 */
+  const float* q;            /* (n, 4) orientation (w, x, y, z), NULL: identity */
+  const float* ang_vel;      /* (n, 1) in 2D or (n, 3) in 3D, NULL: zero */
 } JdemRequest;
 
 typedef struct {
@@ -352,6 +360,9 @@ int jdem_serve_cancel(JdemServer* s, int64_t id);
 int jdem_serve_poll(JdemServer* s, int64_t* ids, int32_t cap, int32_t* count);
 /* Final pos_c, vel, force of a done request (any pointer may be NULL) and its timings. */
 int jdem_serve_result(JdemServer* s, int64_t id, float* pos, float* vel, float* force, JdemRequestInfo* info);
+/* Same, into host arrays of a JdemHostState: pos_c, vel, force, q, ang_vel and
+ * torque are written where not NULL (the other fields are ignored). */
+int jdem_serve_result_state(JdemServer* s, int64_t id, JdemHostState* out, JdemRequestInfo* info);
 /* Free a finished request's buffers. */
 int jdem_serve_release(JdemServer* s, int64_t id);
 /* Wait until no request is pending or active (timeout_s <= 0: no limit). */

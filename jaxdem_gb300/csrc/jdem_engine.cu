@@ -685,10 +685,13 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
 
 // Upload from device arrays already in the reference layout, without any
 // host read: per-system maximum radius and bounding box come from the caller.
-// Spheres only; materials, fixed flags and rotational state take their
-// defaults (material 0, free, identity orientation, zero spin).
+// Spheres only, none fixed.  d_mat (material ids), d_q (orientation) and d_w
+// (angular velocity) may be null: material 0, identity, zero spin; the
+// inertia takes State.create's default from mass and radius.  rot: some
+// system's rotation integrator has a non-trivial state to advance.
 int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
-                                const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s) {
+                                const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s,
+                                const int32_t* d_mat, const float* d_q, const float* d_w, bool rot) {
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
   int rc = plan_grid(rmax_s, lo_s, hi_s);
   if (rc) return rc;
@@ -702,13 +705,16 @@ int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const fl
     else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_frc, 0, N * dim * 4, stream));
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_rad, d_rad, N * 4, k, stream));
     JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_mass, d_mass, N * 4, k, stream));
-    JDEM_CUDA_TRY(this, cudaMemsetAsync(st_mat, 0, N * 4, stream));
+    if (d_mat) JDEM_CUDA_TRY(this, cudaMemcpyAsync(st_mat, d_mat, N * 4, k, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(st_mat, 0, N * 4, stream));
     JDEM_CUDA_TRY(this, cudaMemsetAsync(st_fixed, 0, N, stream));
-    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_w, 0, N * ad * 4, stream));
+    if (d_w) JDEM_CUDA_TRY(this, cudaMemcpyAsync(this->d_w, d_w, N * ad * 4, k, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(this->d_w, 0, N * ad * 4, stream));
     JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
-    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_inertia, 0, N * ad * 4, stream));
-    launch_identity_q((float4*)d_q, (long long)N, stream);
-    rot_active = false;
+    launch_default_inertia(dim, (long long)N, st_mass, st_rad, d_inertia, stream);
+    if (d_q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(this->d_q, d_q, N * 16, k, stream));
+    else launch_identity_q((float4*)this->d_q, (long long)N, stream);
+    rot_active = rot;
     b.NC = 0;
     b.sclump = nullptr;
     launch_pack(dim, b, st_pos, st_vel, st_frc, st_rad, st_mass, st_mat, st_fixed, st_sys, stream);

@@ -42,7 +42,11 @@ struct Req {
   double t_submit = 0, t_admit = 0, t_done = 0;
   float rmax = 0, lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
   float *h_pos = nullptr, *h_vel = nullptr, *h_rad = nullptr, *h_mass = nullptr;  // pinned inputs
+  int32_t* h_mat = nullptr;                                                       // (n) material ids
+  float *h_q = nullptr, *h_w = nullptr;                                           // rotational state
   float *o_pos = nullptr, *o_vel = nullptr, *o_frc = nullptr;                     // pinned outputs
+  float *o_q = nullptr, *o_w = nullptr;
+  bool rot = false;  // a rotation integrator with a non-trivial state (non-identity q or spin)
   int state = REQ_PENDING;
   int status = JDEM_OK;
   bool cancel = false;
@@ -57,14 +61,26 @@ void free_req(Req* r) {
   cudaFreeHost(r->o_pos);
   cudaFreeHost(r->o_vel);
   cudaFreeHost(r->o_frc);
+  cudaFreeHost(r->h_mat);
+  cudaFreeHost(r->h_q);
+  cudaFreeHost(r->h_w);
+  cudaFreeHost(r->o_q);
+  cudaFreeHost(r->o_w);
   delete r;
 }
 
 // Device staging arrays in the reference layout for one batch layout.
 struct Staging {
   float *pos = nullptr, *vel = nullptr, *frc = nullptr, *rad = nullptr, *mass = nullptr;
+  float *mat = nullptr;  // int32 material ids, moved as 4-byte words
+  float *q = nullptr, *w = nullptr;
   long long cap = 0;
 };
+
+void free_staging(Staging& s) {
+  for (float* p : {s.pos, s.vel, s.frc, s.rad, s.mass, s.mat, s.q, s.w}) cudaFree(p);
+  s = Staging{};
+}
 
 }  // namespace
 
@@ -96,6 +112,7 @@ struct JdemServer {
   int64_t unfinished = 0;  // submitted, not yet done / cancelled / failed (guarded by mtx)
   int64_t n_active = 0;    // admitted and not yet finished (guarded by mtx)
   JdemServeStats stats{};
+  std::vector<float> young_eff;  // M * M pair constants of the force law
   std::string err;
 
   int fail(int code, const std::string& m) {
@@ -121,15 +138,11 @@ static int dmalloc(void** p, size_t bytes) {
 int JdemServer::ensure_staging(Staging& s, long long n) {
   if (n <= s.cap) return JDEM_OK;
   long long cap = std::max(n, s.cap + s.cap / 2);
-  cudaFree(s.pos);
-  cudaFree(s.vel);
-  cudaFree(s.frc);
-  cudaFree(s.rad);
-  cudaFree(s.mass);
-  s = Staging{};
-  int d = cfg.dim;
+  free_staging(s);
+  int d = cfg.dim, ad = d == 3 ? 3 : 1;
   if (dmalloc((void**)&s.pos, 4 * cap * d) || dmalloc((void**)&s.vel, 4 * cap * d) ||
-      dmalloc((void**)&s.frc, 4 * cap * d) || dmalloc((void**)&s.rad, 4 * cap) || dmalloc((void**)&s.mass, 4 * cap))
+      dmalloc((void**)&s.frc, 4 * cap * d) || dmalloc((void**)&s.rad, 4 * cap) || dmalloc((void**)&s.mass, 4 * cap) ||
+      dmalloc((void**)&s.mat, 4 * cap) || dmalloc((void**)&s.q, 16 * cap) || dmalloc((void**)&s.w, 4 * cap * ad))
     return fail(JDEM_ERR_OOM, "serve: staging allocation failed");
   s.cap = cap;
   return JDEM_OK;
@@ -161,6 +174,8 @@ int JdemServer::repack(std::vector<Req*>& next) {
     out.pos_c = st[cur].pos;
     out.vel = st[cur].vel;
     out.force = st[cur].frc;
+    out.q = st[cur].q;
+    out.ang_vel = st[cur].w;
     rc = h->download(&out, true);
     if (rc) return fail(rc, std::string("serve: download ") + h->err);
     cur_valid = true;
@@ -169,8 +184,10 @@ int JdemServer::repack(std::vector<Req*>& next) {
   std::vector<JdemSystemDesc> descs;
   std::vector<float> rmax, lo, hi;
   long long o = 0;
-  const int d = cfg.dim;
+  const int d = cfg.dim, ad = d == 3 ? 3 : 1;
+  bool rot = false;
   for (Req* r : next) {
+    rot |= r->rot;
     auto it = old_off.find(r->id);
     if (it != old_off.end()) {
       seg.push_back(it->second);
@@ -184,6 +201,9 @@ int JdemServer::repack(std::vector<Req*>& next) {
         cudaMemsetAsync(st[nxt].frc + o * d, 0, 4 * n * d, s);
         cudaMemcpyAsync(st[nxt].rad + o, r->h_rad, 4 * n, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(st[nxt].mass + o, r->h_mass, 4 * n, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st[nxt].mat + o, r->h_mat, 4 * n, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st[nxt].q + o * 4, r->h_q, 16 * n, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st[nxt].w + o * ad, r->h_w, 4 * n * ad, cudaMemcpyHostToDevice, s);
       }
     }
     descs.push_back(r->desc);
@@ -205,14 +225,16 @@ int JdemServer::repack(std::vector<Req*>& next) {
     cudaFree(d_seg);
     d_seg = nullptr;
     if (dmalloc((void**)&d_seg, sizeof(long long) * seg.size())) return fail(JDEM_ERR_OOM, "serve: segment table");
-    const float* src[5] = {st[cur].pos, st[cur].vel, st[cur].frc, st[cur].rad, st[cur].mass};
-    float* dst[5] = {st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass};
-    int width[5] = {d, d, d, 1, 1};
+    const float* src[8] = {st[cur].pos, st[cur].vel, st[cur].frc, st[cur].rad, st[cur].mass,
+                           st[cur].mat,  st[cur].q,   st[cur].w};
+    float* dst[8] = {st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass,
+                     st[nxt].mat, st[nxt].q,   st[nxt].w};
+    int width[8] = {d, d, d, 1, 1, 1, 4, ad};
     cudaMemcpyAsync(d_seg, seg.data(), sizeof(long long) * seg.size(), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_src, src, sizeof(src), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_dst, dst, sizeof(dst), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_width, width, sizeof(width), cudaMemcpyHostToDevice, s);
-    launch_segcopy(d_seg, nseg, 5, d_src, d_dst, d_width, s);
+    launch_segcopy(d_seg, nseg, 8, d_src, d_dst, d_width, s);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(JDEM_ERR_CUDA, "serve: repack copies failed");
   if (next.empty()) {
@@ -224,7 +246,7 @@ int JdemServer::repack(std::vector<Req*>& next) {
   rc = h->rebind(descs.data(), (int)descs.size());
   if (rc) return fail(rc, std::string("serve: rebind ") + h->err);
   rc = h->upload_resident(st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass, rmax.data(), lo.data(),
-                          hi.data());
+                          hi.data(), (const int32_t*)st[nxt].mat, st[nxt].q, st[nxt].w, rot);
   if (rc) return fail(rc, std::string("serve: upload ") + h->err);
   active = next;
   cur = nxt;
@@ -241,17 +263,21 @@ int JdemServer::finish(std::vector<Req*>& done) {
   out.pos_c = st[cur].pos;
   out.vel = st[cur].vel;
   out.force = st[cur].frc;
+  out.q = st[cur].q;
+  out.ang_vel = st[cur].w;
   int rc = h->download(&out, true);
   if (rc) return fail(rc, std::string("serve: download ") + h->err);
   cur_valid = true;
   long long o = 0;
-  const int d = cfg.dim;
+  const int d = cfg.dim, ad = d == 3 ? 3 : 1;
   for (Req* r : active) {
     if (std::find(done.begin(), done.end(), r) != done.end() && r->desc.n) {
       size_t n = (size_t)r->desc.n;
       cudaMemcpyAsync(r->o_pos, st[cur].pos + o * d, 4 * n * d, cudaMemcpyDeviceToHost, s);
       cudaMemcpyAsync(r->o_vel, st[cur].vel + o * d, 4 * n * d, cudaMemcpyDeviceToHost, s);
       cudaMemcpyAsync(r->o_frc, st[cur].frc + o * d, 4 * n * d, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(r->o_q, st[cur].q + o * 4, 16 * n, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(r->o_w, st[cur].w + o * ad, 4 * n * ad, cudaMemcpyDeviceToHost, s);
     }
     o += r->desc.n;
   }
@@ -443,14 +469,33 @@ int jdem_serve_create(const JdemServeConfig* cfg, JdemServer** out) {
   d.linear_integrator = JDEM_LIN_VERLET;
   d.dt = 1e-3f;
   for (int a = 0; a < 3; ++a) d.box_size[a] = 1.0f;
+  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ) {
+    delete s;
+    return JDEM_ERR_UNSUPPORTED;  // Cundall-Strack needs per-material tables the server does not take
+  }
+  if (cfg->n_materials < 0 || (cfg->n_materials > 0 && !cfg->young_eff)) {
+    delete s;
+    return JDEM_ERR_BAD_ARG;
+  }
   float young = cfg->young > 0 ? cfg->young : 1e3f;
+  const int M = cfg->n_materials > 0 ? cfg->n_materials : 1;
+  try {
+    if (cfg->n_materials > 0) s->young_eff.assign(cfg->young_eff, cfg->young_eff + (size_t)M * M);
+    else s->young_eff.assign(1, young);
+  } catch (...) {
+    delete s;
+    return JDEM_ERR_OOM;
+  }
+  s->cfg.n_materials = M;
+  s->cfg.young_eff = nullptr;  // the server keeps its own copy
   JdemConfig ec{};
   ec.dim = cfg->dim;
   ec.n_systems = 1;
   ec.systems = &d;
   ec.skin = cfg->skin;
-  ec.n_materials = 1;
-  ec.young_eff = &young;
+  ec.n_materials = M;
+  ec.young_eff = s->young_eff.data();
+  ec.force_law = cfg->force_law;
   ec.chunk_steps = s->cfg.chunk_steps;
   ec.device = cfg->device;
   ec.graph_mode = 2;  // the batch changes between epochs: direct launches
@@ -485,12 +530,28 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
     r->lo[a] = 3.4e38f;
     r->hi[a] = -3.4e38f;
   }
+  const int ad = d == 3 ? 3 : 1;
   for (size_t i = 0; i < n; ++i) {
     float rr = req->rad[i];
-    if (!(rr >= 0.0f) || !std::isfinite(rr) || !(req->mass[i] > 0.0f)) {
+    if (!(rr >= 0.0f) || !std::isfinite(rr) || !(req->mass[i] > 0.0f) ||
+        (req->mat_id && (req->mat_id[i] < 0 || req->mat_id[i] >= s->cfg.n_materials))) {
       delete r;
       return JDEM_ERR_BAD_ARG;
     }
+    if (req->system.rotation_integrator != JDEM_ROT_NONE) {
+      // a rotation integrator has work only for a non-identity orientation or a spin
+      if (req->q)
+        r->rot |= req->q[i * 4] != 1.0f || req->q[i * 4 + 1] != 0.0f || req->q[i * 4 + 2] != 0.0f ||
+                  req->q[i * 4 + 3] != 0.0f;
+      if (req->ang_vel)
+        for (int a = 0; a < ad; ++a) r->rot |= req->ang_vel[i * ad + a] != 0.0f;
+    }
+    if (req->ang_vel)
+      for (int a = 0; a < ad; ++a)
+        if (!std::isfinite(req->ang_vel[i * ad + a])) {
+          delete r;
+          return JDEM_ERR_NONFINITE;
+        }
     r->rmax = std::max(r->rmax, rr);
     for (int a = 0; a < d; ++a) {
       float x = req->pos[i * d + a];
@@ -509,10 +570,13 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
     }
   // pinned copies of the inputs and room for the outputs
   size_t vec = 4 * std::max<size_t>(n, 1) * d, sca = 4 * std::max<size_t>(n, 1);
+  size_t q4 = 16 * std::max<size_t>(n, 1), wv = 4 * std::max<size_t>(n, 1) * ad;
   if (cudaMallocHost((void**)&r->h_pos, vec) != cudaSuccess || cudaMallocHost((void**)&r->h_vel, vec) != cudaSuccess ||
       cudaMallocHost((void**)&r->h_rad, sca) != cudaSuccess || cudaMallocHost((void**)&r->h_mass, sca) != cudaSuccess ||
-      cudaMallocHost((void**)&r->o_pos, vec) != cudaSuccess || cudaMallocHost((void**)&r->o_vel, vec) != cudaSuccess ||
-      cudaMallocHost((void**)&r->o_frc, vec) != cudaSuccess) {
+      cudaMallocHost((void**)&r->h_mat, sca) != cudaSuccess || cudaMallocHost((void**)&r->h_q, q4) != cudaSuccess ||
+      cudaMallocHost((void**)&r->h_w, wv) != cudaSuccess || cudaMallocHost((void**)&r->o_pos, vec) != cudaSuccess ||
+      cudaMallocHost((void**)&r->o_vel, vec) != cudaSuccess || cudaMallocHost((void**)&r->o_frc, vec) != cudaSuccess ||
+      cudaMallocHost((void**)&r->o_q, q4) != cudaSuccess || cudaMallocHost((void**)&r->o_w, wv) != cudaSuccess) {
     cudaGetLastError();
     free_req(r);
     return JDEM_ERR_OOM;
@@ -521,8 +585,21 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
   std::memcpy(r->h_vel, req->vel, 4 * n * d);
   std::memcpy(r->h_rad, req->rad, 4 * n);
   std::memcpy(r->h_mass, req->mass, 4 * n);
-  // resident footprint: slot arrays (both copies), staging (both layouts), list
-  r->bytes = n * (size_t)(2 * 96 + 2 * 4 * (3 * d + 2) + 4 * 64);
+  if (req->mat_id) std::memcpy(r->h_mat, req->mat_id, 4 * n);
+  else std::memset(r->h_mat, 0, 4 * n);
+  if (req->q) {
+    std::memcpy(r->h_q, req->q, 16 * n);
+  } else {
+    for (size_t i = 0; i < n; ++i) {
+      r->h_q[i * 4] = 1.0f;
+      r->h_q[i * 4 + 1] = r->h_q[i * 4 + 2] = r->h_q[i * 4 + 3] = 0.0f;
+    }
+  }
+  if (req->ang_vel) std::memcpy(r->h_w, req->ang_vel, 4 * n * ad);
+  else std::memset(r->h_w, 0, 4 * n * ad);
+  // resident footprint: slot arrays (both copies), staging (both layouts, with the
+  // material id and rotational state), both Verlet lists
+  r->bytes = n * (size_t)(2 * 96 + 2 * 4 * (3 * d + 3 + 4 + ad) + 8 * 64);
   if ((double)r->bytes > s->cfg.hbm_budget_bytes) {
     // could never be admitted: reject instead of blocking the queue
     free_req(r);
@@ -594,6 +671,24 @@ int jdem_serve_result(JdemServer* s, int64_t id, float* pos, float* vel, float* 
   return JDEM_OK;
 }
 
+int jdem_serve_result_state(JdemServer* s, int64_t id, JdemHostState* out, JdemRequestInfo* info) {
+  if (!s) return JDEM_ERR_BAD_ARG;
+  const bool want = out && (out->pos_c || out->vel || out->force || out->q || out->ang_vel || out->torque);
+  int rc = jdem_serve_result(s, id, want ? out->pos_c : nullptr, want ? out->vel : nullptr,
+                             want ? out->force : nullptr, info);
+  if (rc || !want) return rc;
+  std::lock_guard<std::mutex> lk(s->mtx);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return JDEM_ERR_BAD_ARG;
+  Req* r = it->second;
+  const size_t n = (size_t)r->desc.n;
+  const int ad = s->cfg.dim == 3 ? 3 : 1;
+  if (out->q) std::memcpy(out->q, r->o_q, 16 * n);
+  if (out->ang_vel) std::memcpy(out->ang_vel, r->o_w, 4 * n * ad);
+  if (out->torque) std::memset(out->torque, 0, 4 * n * ad);  // smooth spheres: no contact torque
+  return JDEM_OK;
+}
+
 int jdem_serve_release(JdemServer* s, int64_t id) {
   if (!s) return JDEM_ERR_BAD_ARG;
   std::lock_guard<std::mutex> lk(s->mtx);
@@ -647,13 +742,7 @@ int jdem_serve_destroy(JdemServer* s) {
   if (s->worker.joinable()) s->worker.join();
   for (auto& kv : s->all) free_req(kv.second);
   for (Req* r : s->graveyard) free_req(r);
-  for (auto& st : s->st) {
-    cudaFree(st.pos);
-    cudaFree(st.vel);
-    cudaFree(st.frc);
-    cudaFree(st.rad);
-    cudaFree(st.mass);
-  }
+  for (auto& st : s->st) free_staging(st);
   cudaFree(s->d_seg);
   cudaFree(s->d_src);
   cudaFree(s->d_dst);

@@ -152,3 +152,56 @@ def test_release_while_batch_continues():
         s.close()
     assert st["completed"] == 2 and st["active"] == 0 and st["pending"] == 0
     assert min_image_diff(r["pos_c"], engine_result(long_)["pos_c"], long_.box_size) <= 1e-5
+
+
+def _engine_alone(w, law, young, mat=None, ang=None, rotation=""):
+    d = w.desc()
+    d["rotation"] = rotation
+    eng = Engine(w.dim, [d], young, skin=default_skin(0.6), force_law=law)
+    try:
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat, ang_vel=ang)
+        eng.step(w.steps)
+        return eng.download()
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_hertz_materials_rotation_alone_equals_in_mix_and_engine(dim):
+    """A Hertz server with two materials: a rotating request (VV-spiral in 3D, spiral in
+    2D, random spins) and a two-material request give the same state alone, in a mix with
+    other requests, and on a standalone engine handle (positions 1e-5, q and spin 2e-6)."""
+    from oracle import dem_ref as R
+
+    k43 = np.asarray(R.hertz_constant(np.array([1e3, 3e3]), np.array([0.3, 0.25])), F32)
+    rot = "verletspiral" if dim == 3 else "spiral"
+    ad = 3 if dim == 3 else 1
+    rng = np.random.default_rng(50 + dim)
+    a = req(1200, 11 + dim, dim=dim, phi=0.45, steps=150)
+    a_mat = rng.integers(0, 2, a.N).astype(np.int32)
+    a_ang = rng.normal(0, 2.0, (a.N, ad)).astype(F32)
+    b = req(900, 21 + dim, dim=dim, phi=0.5, steps=90)
+    b_mat = rng.integers(0, 2, b.N).astype(np.int32)
+
+    def serve(items):
+        s = Server(dim, force_law="hertz", young_eff=k43)
+        try:
+            ids = [s.submit(w, mat_id=m, ang_vel=g, rotation=r) for w, m, g, r in items]
+            s.drain(120)
+            return [s.result(i) for i in ids]
+        finally:
+            s.close()
+
+    alone_a = serve([(a, a_mat, a_ang, rot)])[0]
+    mix = serve([(req(400, 31, dim=dim, steps=40), None, None, ""), (a, a_mat, a_ang, rot),
+                 (b, b_mat, None, ""), (req(2500, 32, dim=dim, phi=0.35, steps=200), None, None, "")])
+    ref_a = _engine_alone(a, "hertz", k43, a_mat, a_ang, rot)
+    ref_b = _engine_alone(b, "hertz", k43, b_mat)
+    for got in (alone_a, mix[1]):
+        assert got["info"]["state"] == "done"
+        assert min_image_diff(got["pos_c"], ref_a["pos_c"], a.box_size) <= 1e-5
+        assert np.allclose(got["q"], ref_a["q"], atol=2e-6)
+        assert np.allclose(got["ang_vel"], ref_a["ang_vel"], atol=2e-6)
+    assert not np.allclose(mix[1]["q"][:, 0], 1.0), "the spins should have rotated the spheres"
+    assert min_image_diff(mix[2]["pos_c"], ref_b["pos_c"], b.box_size) <= 1e-5
+    assert np.allclose(mix[2]["q"], np.array([1, 0, 0, 0], F32))
