@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 8
+#define JDEM_ABI_VERSION 9
 
 enum {
   JDEM_OK = 0,
@@ -109,6 +109,8 @@ typedef struct {
                                    r_i + r_j + prune_skin, rebuilt from the full list whenever
                                    the drift since its build exceeds prune_skin / 2.
                                    0: skin / 3; < 0: off (every step walks the full list) */
+  int32_t brick_particles;      /* list build: particles per brick of cells staged in shared
+                                   memory (<= 0: 240) */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

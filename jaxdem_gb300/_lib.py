@@ -77,6 +77,7 @@ class Config(C.Structure):
         ("force_law", C.c_int32),
         ("material_props", C.POINTER(C.c_float)),
         ("prune_skin", C.c_float),
+        ("brick_particles", C.c_int32),
     ]
 
 
@@ -206,7 +207,8 @@ class Engine:
     def __init__(self, dim: int, systems: Sequence[dict], young_eff: np.ndarray, skin: float = 0.0,
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
                  device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring",
-                 material_props: Optional[np.ndarray] = None, prune_skin: float = 0.0):
+                 material_props: Optional[np.ndarray] = None, prune_skin: float = 0.0,
+                 brick_particles: int = 0):
         """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k,
         (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``), or the damping ratio
         beta for ``"cundallstrack"``, which also takes ``material_props`` (M, 4)
@@ -259,6 +261,8 @@ class Engine:
         cfg.force_law = FORCE_LAW[force_law]
         # inner-list margin of the dynamic pruning (0: skin / 3, < 0: off)
         cfg.prune_skin = float(prune_skin)
+        # particles per shared-memory brick of the list build (0: 240)
+        cfg.brick_particles = int(brick_particles)
         self.force_law = force_law
         self._props = None
         if material_props is not None:

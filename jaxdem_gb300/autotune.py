@@ -1,12 +1,20 @@
-"""Autotuner for the engine's tunable shape: the binning/list skin.
+"""Autotuner for the engine's tunable shapes.
 
-The skin trades list length (pair tests every step grow as (2r + skin)^3)
-against the re-sort rate (a re-sort is due when the accumulated displacement
-reaches skin / 2).  The best value depends on density, temperature and size,
-so it is measured: a few candidate skins each run a short timed chunk on the
-actual system, and the fastest wins.  Results are cached per configuration
-class (dimension, log2 particle bucket, density bucket, mean speed bucket)
-in a JSON file, so repeated runs of similar workloads skip the search.
+* skin: list length (pair tests every step grow as (2r + skin)^3) against the
+  re-sort rate (a re-sort is due when the accumulated displacement reaches
+  skin / 2);
+* prune skin: the inner list of the dynamic pruning, shorter with a small
+  margin but rebuilt from the full list more often (off, or a fraction of the
+  skin);
+* brick size: particles per shared-memory brick of the list build (larger
+  bricks stage relatively fewer halo cells but fill fewer blocks).
+
+The best values depend on density, temperature and size, so they are
+measured: a coordinate search times a short chunk of steps on the actual
+system for each candidate of one shape at a time (skin, then prune skin, then
+brick size), keeping the fastest.  Results are cached per configuration class
+(dimension, log2 particle bucket, density bucket, mean speed bucket) in a JSON
+file, so repeated runs of similar workloads skip the search.
 """
 
 from __future__ import annotations
@@ -91,3 +99,63 @@ def workload_key(w) -> str:
     phi = float(volume(w.rad, w.dim).astype(np.float64).sum() / vol) if vol > 0 else 0.0
     vrms = float(np.sqrt(np.mean(np.asarray(w.vel, np.float64) ** 2))) if w.N else 0.0
     return config_key(w.dim, w.N, phi, vrms, w.domain)
+
+
+# prune skin as a fraction of the skin (-1: pruning off) and list-build brick sizes
+PRUNE_CANDIDATES = (-1.0, 0.2, 1.0 / 3.0, 0.5)
+BRICK_CANDIDATES = (120, 240, 480)
+
+
+def _time_chunk(make_engine, upload, params, steps):
+    eng = make_engine(**params)
+    try:
+        upload(eng)
+        eng.step(max(10, steps // 3))  # warm-up: first re-sort, graph capture
+        eng.sync()
+        t0 = time.perf_counter()
+        eng.step(steps)
+        return (time.perf_counter() - t0) / steps
+    finally:
+        eng.close()
+
+
+def tune_shapes(make_engine: Callable[..., "object"], upload: Callable[["object"], None], rmax: float,
+                n_particles: int, key: Optional[str] = None, steps: int = 60, use_cache: bool = True) -> tuple[dict, dict]:
+    """Coordinate search over (skin, prune skin, brick size); returns (best, timings).
+
+    ``make_engine(skin=..., prune_skin=..., brick_particles=...)`` builds an engine and
+    ``upload(engine)`` loads the state.  ``best`` holds the three arguments; ``timings``
+    the seconds per step of every candidate, per shape.  The prune skin and brick size
+    only matter above 32768 particles (the fused list kernel and the brick build), so
+    smaller systems tune the skin alone.
+    """
+    cache = _load() if use_cache else {}
+    ckey = None if key is None else "shapes:" + key
+    if ckey is not None and ckey in cache:
+        c = cache[ckey]
+        return ({"skin": c["skin_rel"] * rmax, "prune_skin": c["prune_rel"] * c["skin_rel"] * rmax
+                 if c["prune_rel"] > 0 else -1.0, "brick_particles": int(c["brick"])}, c.get("timings", {}))
+    timings = {"skin": {}, "prune": {}, "brick": {}}
+    large = n_particles > 32768
+    base = {"prune_skin": 0.0, "brick_particles": 240}
+    for c in CANDIDATES:
+        timings["skin"][str(c)] = _time_chunk(make_engine, upload, {"skin": c * rmax, **base}, steps)
+    skin_rel = float(min(timings["skin"], key=timings["skin"].get))
+    prune_rel, brick = 1.0 / 3.0, 240
+    if large:
+        for pr in PRUNE_CANDIDATES:
+            ps = -1.0 if pr < 0 else pr * skin_rel * rmax
+            timings["prune"][str(round(pr, 3))] = _time_chunk(
+                make_engine, upload, {"skin": skin_rel * rmax, "prune_skin": ps, "brick_particles": 240}, steps)
+        prune_rel = float(min(timings["prune"], key=timings["prune"].get))
+        ps = -1.0 if prune_rel < 0 else prune_rel * skin_rel * rmax
+        for bk in BRICK_CANDIDATES:
+            timings["brick"][str(bk)] = _time_chunk(
+                make_engine, upload, {"skin": skin_rel * rmax, "prune_skin": ps, "brick_particles": bk}, steps)
+        brick = int(min(timings["brick"], key=timings["brick"].get))
+    best = {"skin": skin_rel * rmax, "prune_skin": -1.0 if prune_rel < 0 else prune_rel * skin_rel * rmax,
+            "brick_particles": brick}
+    if ckey is not None:
+        cache[ckey] = {"skin_rel": skin_rel, "prune_rel": prune_rel, "brick": brick, "timings": timings}
+        _store(cache)
+    return best, timings

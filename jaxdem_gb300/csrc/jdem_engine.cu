@@ -155,6 +155,7 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   nl_request = cfg->neighbor_list;
   if (!std::isfinite(cfg->prune_skin)) return fail(JDEM_ERR_BAD_ARG, "config: prune_skin must be finite");
   prune_req = cfg->prune_skin;
+  brick_tt = cfg->brick_particles > 0 ? (double)cfg->brick_particles : 240.0;
   int rc0 = set_systems(cfg->systems, S);
   if (rc0) return rc0;
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
@@ -392,7 +393,7 @@ int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* h
 }
 
 // Tiles of the brick list build (jdem_tiles.cu) for every system: bricks of
-// cells holding about 240 particles, near-cubic so the staged stencil region
+// cells holding about brick_tt particles (240 unless configured), near-cubic so the staged stencil region
 // (the brick grown by one cell per side) is small against the brick; a system
 // smaller than one brick is one tile.  Free domains re-grid on the device at
 // every re-sort, so a handle with one keeps the per-slot list build (no tiles).
@@ -400,7 +401,7 @@ int JdemHandle::plan_tiles() {
   std::vector<TileDesc> t;
   int nst = 0, nv = 0, nrows = 0;
   if (!any_free && use_nl) {
-    const double TT = 240.0;
+    const double TT = brick_tt;
     constexpr long long kMaxNV = 2048, kMaxHomeRows = 256, kMaxRows = 512;
     double stage_max = 0.0;
     long long nv_max = 0, rows_max = 0;
