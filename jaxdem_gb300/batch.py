@@ -16,6 +16,7 @@ import numpy as np
 
 from . import autotune
 from ._lib import Engine
+from .state import Quaternion
 from .workloads import K_SPRING, Workload
 
 F32 = np.float32
@@ -75,7 +76,10 @@ class BatchedSystems:
 
 def step_many(states, systems, n: int):
     """``System.step`` over a list of (state, system) pairs of possibly different N,
-    in one batched device handle per dimension; returns lists of states and systems."""
+    in one batched device handle per dimension; returns lists of states and systems.
+    Handles are cached by the batch's static configuration (the systems' sizes,
+    domains, integrators, force law and materials), so repeated calls on batches of
+    the same shape reuse device memory and captured CUDA graphs."""
     from . import session
     from .state import State
 
@@ -95,34 +99,29 @@ def step_many(states, systems, n: int):
             if lk != law or not np.array_equal(yk, young) or (props is not None and not np.array_equal(pk, props)):
                 raise NotImplementedError("systems of one batch must share the force law and material table")
         skin = max(session._skin(states[k], systems[k]) for k in idx)
-        eng = Engine(dim, descs, young, skin=skin, force_law=law, material_props=props)
-        try:
-            cat = lambda f: np.concatenate([np.asarray(f(states[k])) for k in idx])  # noqa: E731
-            ad = 3 if dim == 3 else 1
-            eng.upload(pos=cat(lambda s: s.pos_c), rad=cat(lambda s: s.rad), mass=cat(lambda s: s.mass),
-                       vel=cat(lambda s: s.vel), force=cat(lambda s: s.force),
-                       q=cat(lambda s: s.q.as_array()), ang_vel=cat(lambda s: s.ang_vel.reshape(-1, ad)),
-                       torque=cat(lambda s: s.torque.reshape(-1, ad)),
-                       inertia=cat(lambda s: s.inertia.reshape(-1, ad)), mat_id=cat(lambda s: s.mat_id),
-                       fixed=cat(lambda s: s.fixed))
-            eng.step(n)
-            res = eng.download()
-            off = 0
-            for k in idx:
-                st = states[k]
-                N = st.N
-                sub = State.copy(st)
-                sub.pos_c = res["pos_c"][off:off + N].copy()
-                sub.vel = res["vel"][off:off + N].copy()
-                sub.force = res["force"][off:off + N].copy()
-                from .state import Quaternion
-
-                sub.q = Quaternion.from_array(res["q"][off:off + N])
-                sub.ang_vel = res["ang_vel"][off:off + N].reshape(st.ang_vel.shape)
-                sub.torque = res["torque"][off:off + N].reshape(st.torque.shape)
-                out_states[k] = sub
-                out_systems[k] = session._advance_system(systems[k], eng, n, False, index=idx.index(k))
-                off += N
-        finally:
-            eng.close()
+        eng = session.cached_engine(dim, descs, young, skin=skin, law=law, props=props)
+        cat = lambda f: np.concatenate([np.asarray(f(states[k])) for k in idx])  # noqa: E731
+        ad = 3 if dim == 3 else 1
+        eng.upload(pos=cat(lambda s: s.pos_c), rad=cat(lambda s: s.rad), mass=cat(lambda s: s.mass),
+                   vel=cat(lambda s: s.vel), force=cat(lambda s: s.force),
+                   q=cat(lambda s: s.q.as_array()), ang_vel=cat(lambda s: s.ang_vel.reshape(-1, ad)),
+                   torque=cat(lambda s: s.torque.reshape(-1, ad)),
+                   inertia=cat(lambda s: s.inertia.reshape(-1, ad)), mat_id=cat(lambda s: s.mat_id),
+                   fixed=cat(lambda s: s.fixed))
+        eng.step(n)
+        res = eng.download()
+        off = 0
+        for k in idx:
+            st = states[k]
+            N = st.N
+            sub = State.copy(st)
+            sub.pos_c = res["pos_c"][off:off + N].copy()
+            sub.vel = res["vel"][off:off + N].copy()
+            sub.force = res["force"][off:off + N].copy()
+            sub.q = Quaternion.from_array(res["q"][off:off + N])
+            sub.ang_vel = res["ang_vel"][off:off + N].reshape(st.ang_vel.shape)
+            sub.torque = res["torque"][off:off + N].reshape(st.torque.shape)
+            out_states[k] = sub
+            out_systems[k] = session._advance_system(systems[k], eng, n, False, index=idx.index(k))
+            off += N
     return out_states, out_systems

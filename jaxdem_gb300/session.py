@@ -136,25 +136,20 @@ def pair_law(system) -> tuple:
     return law, np.asarray(mt.young_eff, F32), None
 
 
-def engine_for(state: State, system) -> Engine:
-    """Cached engine handle for this static configuration."""
-    _check_supported(state, system)
-    descs = _descs(state, system)
-    law, young, props = pair_law(system)
-    W = _bond_width(state)
-    skin = _skin(state, system)
-    # a NeighborList collider's max_neighbors is the initial list capacity
-    cap = getattr(system.collider, "max_neighbors", None)
-    nl = int(cap) if cap else True
-    key = (state.dim, W, bool(system.interact_same_bond_id), round(skin, 7), nl, law, young.tobytes(),
+def cached_engine(dim: int, descs: list, young: np.ndarray, *, skin: float, law: str = "spring",
+                  props: Optional[np.ndarray] = None, bond_width: int = 0, interact_same_bond_id: bool = False,
+                  neighbor_list=True) -> Engine:
+    """Engine handle for this static configuration, reused across calls (device memory and
+    captured CUDA graphs stay; each call uploads its own state)."""
+    key = (dim, bond_width, bool(interact_same_bond_id), round(skin, 7), neighbor_list, law, young.tobytes(),
            None if props is None else props.tobytes(),
            tuple((d["n"], d["domain"], d["linear"], d["rotation"], d["dt"], tuple(map(float, d["box_size"])),
                   tuple(map(float, d["anchor"])), d["restitution"], tuple(map(float, d["gravity"])),
                   d["cell_size"], d["search_range"]) for d in descs))
     eng = _CACHE.get(key)
     if eng is None:
-        eng = Engine(state.dim, descs, young, skin=skin, bond_width=W,
-                     interact_same_bond_id=bool(system.interact_same_bond_id), neighbor_list=nl, force_law=law,
+        eng = Engine(dim, descs, young, skin=skin, bond_width=bond_width,
+                     interact_same_bond_id=bool(interact_same_bond_id), neighbor_list=neighbor_list, force_law=law,
                      material_props=props)
         _CACHE[key] = eng
         while len(_CACHE) > _CACHE_MAX:
@@ -163,6 +158,18 @@ def engine_for(state: State, system) -> Engine:
     else:
         _CACHE.move_to_end(key)
     return eng
+
+
+def engine_for(state: State, system) -> Engine:
+    """Cached engine handle for this static configuration."""
+    _check_supported(state, system)
+    descs = _descs(state, system)
+    law, young, props = pair_law(system)
+    # a NeighborList collider's max_neighbors is the initial list capacity
+    cap = getattr(system.collider, "max_neighbors", None)
+    return cached_engine(state.dim, descs, young, skin=_skin(state, system), law=law, props=props,
+                         bond_width=_bond_width(state), interact_same_bond_id=bool(system.interact_same_bond_id),
+                         neighbor_list=int(cap) if cap else True)
 
 
 def clear_cache() -> None:

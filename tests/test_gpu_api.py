@@ -89,6 +89,15 @@ def test_step_many_uneven_systems():
         box = w.box_size if w.domain == "periodic" else None
         assert min_image_diff(st2.pos_c, alone.pos_c, box) <= 1e-5
         assert int(sy2.step_count) == 25
+    # a second call on batches of the same shape reuses the cached handle: same results,
+    # no new handle (the input states are not modified by the first call)
+    from jaxdem_gb300 import session
+
+    n_handles = len(session._CACHE)
+    again, _ = step_many([i[1] for i in items], [i[2] for i in items], 25)
+    assert len(session._CACHE) == n_handles
+    for a, b in zip(sts, again):
+        assert np.array_equal(a.pos_c, b.pos_c) and np.array_equal(a.vel, b.vel)
 
 
 def test_collider_slot_and_pair_forces():
