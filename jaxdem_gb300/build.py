@@ -2,8 +2,12 @@
 
 ``build()`` compiles every ``csrc/*.cu`` translation unit in parallel and
 links ``_lib/libjdem_gb300.so``.  Flags: ``-fmad=false`` keeps each float
-product and sum rounding as written (the kernels restate the reference's
-float32 operation order); ``-lineinfo`` for profiler source correlation.
+product and sum rounding as written in the translation units whose kernels
+restate the reference's float32 arithmetic (contact forces and their pair
+predicate, integrators, domains, energies, the neighbour-list API); the list
+build (``jdem_tiles.cu``, tests against a widened cutoff and fuses its own
+multiply-adds) and the host-only units compile with contraction allowed.
+``-lineinfo`` for profiler source correlation.
 
 The XLA FFI handlers (``csrc/ffi/jdem_xla_ffi.cc``) are built into
 ``_lib/libjdem_xla_ffi.so`` only where jaxlib's FFI headers exist: the
@@ -23,7 +27,9 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libjdem_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# translation units free of reference arithmetic: multiply-add contraction allowed
+CONTRACT_OK = {"jdem_tiles.cu", "jdem_engine.cu", "jdem_serve.cu", "jdem_rollout.cu"}
 
 
 def nvcc() -> str:
@@ -57,7 +63,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: Path) -> Path:
         obj = obj_dir / (src.stem + ".o")
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *inc, "-c", str(src), "-o", str(obj)]
+        fmad = [] if src.name in CONTRACT_OK else ["-fmad=false"]
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *inc, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
