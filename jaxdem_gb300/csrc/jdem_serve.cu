@@ -47,6 +47,7 @@ struct Req {
   float *o_pos = nullptr, *o_vel = nullptr, *o_frc = nullptr;                     // pinned outputs
   float *o_q = nullptr, *o_w = nullptr;
   bool rot = false;  // a rotation integrator with a non-trivial state (non-identity q or spin)
+  char* block = nullptr;  // one page-locked allocation holding every array above
   int state = REQ_PENDING;
   int status = JDEM_OK;
   bool cancel = false;
@@ -54,18 +55,7 @@ struct Req {
 };
 
 void free_req(Req* r) {
-  cudaFreeHost(r->h_pos);
-  cudaFreeHost(r->h_vel);
-  cudaFreeHost(r->h_rad);
-  cudaFreeHost(r->h_mass);
-  cudaFreeHost(r->o_pos);
-  cudaFreeHost(r->o_vel);
-  cudaFreeHost(r->o_frc);
-  cudaFreeHost(r->h_mat);
-  cudaFreeHost(r->h_q);
-  cudaFreeHost(r->h_w);
-  cudaFreeHost(r->o_q);
-  cudaFreeHost(r->o_w);
+  cudaFreeHost(r->block);
   delete r;
 }
 
@@ -569,17 +559,36 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
       r->hi[a] = 1.0f;
     }
   // pinned copies of the inputs and room for the outputs
-  size_t vec = 4 * std::max<size_t>(n, 1) * d, sca = 4 * std::max<size_t>(n, 1);
-  size_t q4 = 16 * std::max<size_t>(n, 1), wv = 4 * std::max<size_t>(n, 1) * ad;
-  if (cudaMallocHost((void**)&r->h_pos, vec) != cudaSuccess || cudaMallocHost((void**)&r->h_vel, vec) != cudaSuccess ||
-      cudaMallocHost((void**)&r->h_rad, sca) != cudaSuccess || cudaMallocHost((void**)&r->h_mass, sca) != cudaSuccess ||
-      cudaMallocHost((void**)&r->h_mat, sca) != cudaSuccess || cudaMallocHost((void**)&r->h_q, q4) != cudaSuccess ||
-      cudaMallocHost((void**)&r->h_w, wv) != cudaSuccess || cudaMallocHost((void**)&r->o_pos, vec) != cudaSuccess ||
-      cudaMallocHost((void**)&r->o_vel, vec) != cudaSuccess || cudaMallocHost((void**)&r->o_frc, vec) != cudaSuccess ||
-      cudaMallocHost((void**)&r->o_q, q4) != cudaSuccess || cudaMallocHost((void**)&r->o_w, wv) != cudaSuccess) {
+  // page-locked copies of the inputs and room for the outputs, carved from one
+  // allocation (page-locking is slow: one call per request, not one per array)
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t vec = up(4 * std::max<size_t>(n, 1) * d), sca = up(4 * std::max<size_t>(n, 1));
+  size_t q4 = up(16 * std::max<size_t>(n, 1)), wv = up(4 * std::max<size_t>(n, 1) * ad);
+  if (cudaMallocHost((void**)&r->block, 5 * vec + 3 * sca + 2 * q4 + 2 * wv) != cudaSuccess) {
     cudaGetLastError();
+    r->block = nullptr;
     free_req(r);
     return JDEM_ERR_OOM;
+  }
+  {
+    char* c = r->block;
+    auto take = [&](size_t b) {
+      char* q = c;
+      c += b;
+      return q;
+    };
+    r->h_pos = (float*)take(vec);
+    r->h_vel = (float*)take(vec);
+    r->o_pos = (float*)take(vec);
+    r->o_vel = (float*)take(vec);
+    r->o_frc = (float*)take(vec);
+    r->h_rad = (float*)take(sca);
+    r->h_mass = (float*)take(sca);
+    r->h_mat = (int32_t*)take(sca);
+    r->h_q = (float*)take(q4);
+    r->o_q = (float*)take(q4);
+    r->h_w = (float*)take(wv);
+    r->o_w = (float*)take(wv);
   }
   std::memcpy(r->h_pos, req->pos, 4 * n * d);
   std::memcpy(r->h_vel, req->vel, 4 * n * d);
