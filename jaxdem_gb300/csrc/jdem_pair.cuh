@@ -176,38 +176,43 @@ __device__ __forceinline__ float integrate_particle(const Bufs& b, int mode, lon
   bool fixed = (tg & TAG_FIXED) != 0u;
   float fr = fixed ? 0.0f : 1.0f;
   float p[3] = {pi.x, pi.y, pi.z}, v[3] = {v4.x, v4.y, v4.z};
+  // the system's fields in registers: the stores below could alias the table for
+  // the compiler, which would otherwise load them again
+  const int lin = sp.lin, domain = sp.domain;
+  const float dt = sp.dt;
+  // the Verlet half kick dt * 0.5 / m (velocity_verlet.py:58-60, 92-94) is the same
+  // before and after the force: one division
+  const float sc_half = dt * 0.5f / m;
   // ForceManager.apply: F_contact + F_part(0) + gravity * (mass / count)
 #pragma unroll
   for (int a = 0; a < DIM; ++a) F[a] = (F[a] + 0.0f) + sp.gravity[a] * (m / 1.0f);
-  if (sp.lin == LIN_VERLET) {
-    float sc = sp.dt * 0.5f / m;
+  if (lin == LIN_VERLET) {
 #pragma unroll
-    for (int a = 0; a < DIM; ++a) v[a] = v[a] + F[a] * sc * fr;
-  } else if (sp.lin == LIN_EULER) {
-    float sc = sp.dt / m;
+    for (int a = 0; a < DIM; ++a) v[a] = v[a] + F[a] * sc_half * fr;
+  } else if (lin == LIN_EULER) {
+    float sc = dt / m;
 #pragma unroll
     for (int a = 0; a < DIM; ++a) {
       v[a] = v[a] + F[a] * sc * fr;
-      p[a] = p[a] + sp.dt * v[a];
+      p[a] = p[a] + dt * v[a];
     }
   }
   // nothing on the step path reads the force back: a streaming store
   __stcs(&b.frc[sel][t], make_float4(F[0], F[1], F[2], 0.0f));
   if (base_mode == MODE_STEP) {
-    if ((mode & MODE_BBOX) && sp.domain == DOM_FREE) {
+    if ((mode & MODE_BBOX) && domain == DOM_FREE) {
 #pragma unroll
       for (int a = 0; a < DIM; ++a) {
         atomicMin((unsigned int*)&b.bbox[s * 6 + a], f2ord(p[a] - pi.w));
         atomicMax((unsigned int*)&b.bbox[s * 6 + 3 + a], f2ord(p[a] + pi.w));
       }
     }
-    if (sp.domain == DOM_REFLECT) reflect_sphere<DIM>(sp, p, v, F, pi.w, m, fixed);
-    if (sp.lin == LIN_VERLET) {
-      float sc = sp.dt * 0.5f / m;
+    if (domain == DOM_REFLECT) reflect_sphere<DIM>(sp, p, v, F, pi.w, m, fixed);
+    if (lin == LIN_VERLET) {
 #pragma unroll
       for (int a = 0; a < DIM; ++a) {
-        v[a] = v[a] + F[a] * sc * fr;
-        p[a] = p[a] + sp.dt * v[a];
+        v[a] = v[a] + F[a] * sc_half * fr;
+        p[a] = p[a] + dt * v[a];
       }
     }
   }

@@ -88,7 +88,7 @@ def test_cancellation_leaves_others_untouched():
 
 def test_hbm_budget_limits_concurrency():
     ws = [req(1000, 20 + k, steps=60) for k in range(4)]
-    s = Server(3, hbm_budget_gb=0.0008)  # room for one 1000-particle request
+    s = Server(3, hbm_budget_gb=0.0012)  # room for one 1000-particle request (about 0.86 MB), not two
     try:
         ids = [s.submit(w) for w in ws]
         s.drain(120)
