@@ -539,12 +539,14 @@ template <int DIM, bool NL, bool GENERAL, int LAW>
 // (84.5 us against 90 us at 64 registers on 1M spheres).
 __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  const bool use_list = NL && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  // control fields earlier kernels set and this one only reads (of status only the
+  // list-overflow bit, which the list build sets): read-only path
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
+  const bool use_list = NL && (ld_nc_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
   // dynamic pruning (uniform over the launch): a prune pass walks the full
   // list and writes the inner one; the other passes walk the inner list
   const bool pruning = use_list && b.nbr2 != nullptr;
-  const bool prune = pruning && (ld_cg_u32(&b.ctl->prune) | ld_cg_u32(&b.ctl->nl_dirty)) != 0u;
+  const bool prune = pruning && (ld_nc_u32(&b.ctl->prune) | ld_nc_u32(&b.ctl->nl_dirty)) != 0u;
   float d2max = 0.0f;
   if (t < b.P) {
     const long long row = ((t >> 5) * b.nl_cap) * 32 + (t & 31);
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(128, 10) k_force(Bufs b, int mode) {
     d2max = particle_step<DIM, GENERAL, LAW>(b, mode, t, sel, ps, use_list, nb, n, 32,
                                              prune ? b.nbr2 + row : nullptr, prune ? b.ncnt2 + t : nullptr);
   }
-  if ((mode & 7) != MODE_FORCE_ONLY) warp_disp(b.ctl, d2max);
+  if ((mode & 7) != MODE_FORCE_ONLY) block_disp<128>(b.ctl, d2max);
 }
 
 // Small systems: with too few slots to fill the GPU the duration of k_force is

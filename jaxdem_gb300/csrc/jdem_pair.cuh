@@ -25,6 +25,24 @@ __device__ __forceinline__ void warp_disp(Ctl* ctl, float d2) {
     atomicMax(&ctl->maxdisp2, __float_as_uint(d2));
 }
 
+// Block max of the squared displacement (NT threads a block): one L2 read of the
+// kernel-wide maximum, and rarely one atomic, per block instead of per warp --
+// every warp of a large launch would otherwise poll the same L2 line.  Every
+// thread of the block must call it.
+template <int NT>
+__device__ __forceinline__ void block_disp(Ctl* ctl, float d2) {
+  __shared__ float s_w[NT / 32];
+  d2 = warp_max(d2);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = d2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = s_w[0];
+#pragma unroll
+    for (int w = 1; w < NT / 32; ++w) m = s_w[w] > m ? s_w[w] : m;
+    if (m > 0.0f && m > __uint_as_float(__ldcg(&ctl->maxdisp2))) atomicMax(&ctl->maxdisp2, __float_as_uint(m));
+  }
+}
+
 // Minimum-image displacement and squared distance, in the reference's order
 // (periodic.py:74-79: d - box * round(d / box)).  When every |d / box| <= 0.5
 // the rounded multiple is +-0 and d - box * (+-0) == d, so the correction is
