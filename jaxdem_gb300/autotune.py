@@ -61,37 +61,6 @@ def _store(d: dict) -> None:
         pass
 
 
-def tune_skin(make_engine: Callable[[float], "object"], upload: Callable[["object"], None], rmax: float,
-              key: Optional[str] = None, steps: int = 60, candidates: Sequence[float] = CANDIDATES,
-              use_cache: bool = True) -> tuple[float, dict]:
-    """Return (best skin, {skin: seconds per step}).
-
-    ``make_engine(skin)`` builds an engine, ``upload(engine)`` loads the
-    state; each candidate runs ``steps`` steps after a warm-up chunk.
-    """
-    cache = _load() if use_cache else {}
-    if key is not None and key in cache:
-        return float(cache[key]["skin_rel"]) * rmax, cache[key].get("timings", {})
-    timings = {}
-    for c in candidates:
-        skin = c * rmax
-        eng = make_engine(skin)
-        try:
-            upload(eng)
-            eng.step(max(10, steps // 3))  # warm-up: first re-sort, graph capture
-            eng.sync()
-            t0 = time.perf_counter()
-            eng.step(steps)
-            timings[c] = (time.perf_counter() - t0) / steps
-        finally:
-            eng.close()
-    best = min(timings, key=timings.get)
-    if key is not None:
-        cache[key] = {"skin_rel": best, "timings": {str(k): v for k, v in timings.items()}}
-        _store(cache)
-    return best * rmax, timings
-
-
 def workload_key(w) -> str:
     from .workloads import volume
 
@@ -110,7 +79,9 @@ def _time_chunk(make_engine, upload, params, steps):
     eng = make_engine(**params)
     try:
         upload(eng)
-        eng.step(max(10, steps // 3))  # warm-up: first re-sort, graph capture
+        # warm-up with the timed call itself: the first re-sort, and every CUDA graph the
+        # timed call launches is captured before the clock starts
+        eng.step(steps)
         eng.sync()
         t0 = time.perf_counter()
         eng.step(steps)

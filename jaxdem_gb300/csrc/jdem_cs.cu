@@ -122,8 +122,8 @@ __global__ void k_cs_force(Bufs b) {
   constexpr int AD = DIM == 3 ? 3 : 1;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  const bool use_list = b.nl_cap > 0 && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
+  const bool use_list = b.nl_cap > 0 && (ld_nc_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
   const float4* __restrict__ P = b.pos[ps];
   const float4 pi = P[t];
   const float4 vi4 = b.vel[sel][t];
@@ -182,7 +182,7 @@ __global__ void k_cs_step(Bufs b, int mode) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   float d2max = 0.0f;
   if (t < b.P) {
-    const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+    const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
     const float4 pi = b.pos[ps][t];
     const uint32_t tg = b.tag[sel][t];
     const SysParams& sp = b.sys[tg & TAG_SYS_MASK];

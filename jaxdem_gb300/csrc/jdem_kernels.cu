@@ -86,7 +86,7 @@ __global__ void k_unpack(Bufs b, float* __restrict__ pos, float* __restrict__ ve
                          float* __restrict__ frc) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   long long i = b.orig[sel][t];
   // a null destination skips that field (trajectory frames select fields)
   if (pos) {
@@ -122,11 +122,11 @@ __global__ void k_bbox_reset(unsigned int* __restrict__ bb, int S) {
 // one block per free system; grid capped at the system's cell capacity.
 template <int DIM>
 __global__ void k_grid_free(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   int s = blockIdx.x;
   SysParams& sp = b.sys[s];
   if (sp.domain != DOM_FREE) return;
-  unsigned int ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int ps = ld_nc_u32(&b.ctl->pos_sel);
   float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
   for (long long t = sp.p0 + threadIdx.x; t < sp.p0 + sp.np; t += blockDim.x) {
     float4 p = b.pos[ps][t];
@@ -184,10 +184,10 @@ __global__ void k_grid_free(Bufs b) {
 // from the atomic and is made deterministic by k_cellsort).
 template <int DIM>
 __global__ void k_bin(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   float4 p = b.pos[ps][t];
   uint32_t tg = b.tag[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
@@ -243,7 +243,7 @@ __device__ __forceinline__ int block_excl_scan(int v, int* sh, int& total) {
 }
 
 __global__ void k_scan_reduce(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   __shared__ int sh[32];
   long long base = (long long)blockIdx.x * SCAN_TILE;
   int s = 0;
@@ -258,7 +258,7 @@ __global__ void k_scan_reduce(Bufs b) {
 }
 
 __global__ void k_scan_top(Bufs b, int nblk) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   __shared__ int sh[32];
   // one block of 1024 threads, each owning a run of ceil(nblk/1024) entries
   int per = (nblk + blockDim.x - 1) / blockDim.x;
@@ -275,7 +275,7 @@ __global__ void k_scan_top(Bufs b, int nblk) {
 }
 
 __global__ void k_scan_down(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   __shared__ int sh[32];
   long long base = (long long)blockIdx.x * SCAN_TILE;
   int v[SCAN_V];
@@ -298,7 +298,7 @@ __global__ void k_scan_down(Bufs b) {
 }
 
 __global__ void k_scatter(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
   int key = b.key_tmp[t];
@@ -308,10 +308,10 @@ __global__ void k_scatter(Bufs b) {
 // Per cell: order the cell's slots by original index (the stable order of
 // lax.sort([hash, iota]), cell_list.py:64) and clear the occupancy counter.
 __global__ void k_cellsort(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= b.C) return;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel);
   int a = b.cell_start[c], e = b.cell_start[c + 1];
   b.cnt[c] = 0;
   const int32_t* orig = b.orig[sel];
@@ -330,9 +330,9 @@ __global__ void k_cellsort(Bufs b) {
 // Gather every slot array into the spare copy in sorted order (k_sort_fin
 // then flips the copies).
 __global__ void k_gather(Bufs b) {
-  if (ld_cg_u32(&b.ctl->need_rebuild) == 0u) return;
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   if (u < b.P) {
     int t = __ldcs(&b.perm_tmp[u]);  // old-order records are read once: streaming loads
     const float4 p = __ldcs(&b.pos[ps][t]);
@@ -385,7 +385,7 @@ __global__ void k_sort_fin(Ctl* ctl) {
 template <int DIM>
 __global__ void k_pre(Bufs b, int mode) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   float d2 = 0.0f;
   if (t < b.P) {
     float4 p4 = b.pos[ps][t];
@@ -441,10 +441,10 @@ __global__ void k_pre(Bufs b, int mode) {
 // per k.  Entries are in ascending slot order within each stencil row.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
-  if (ld_cg_u32(&b.ctl->nl_dirty) == 0u) return;
+  if (ld_nc_u32(&b.ctl->nl_dirty) == 0u) return;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel);
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel);
   const SysParams& sp = b.sys[b.tag[sel][t] & TAG_SYS_MASK];
   const bool per = sp.domain == DOM_PERIODIC;
   // Wrapped positions with one image shift per stencil row (every grid axis
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
   // test only selects list members, so it may round differently from the
   // force: the cutoff is widened by 1e-4 relative to stay a superset.
   const bool shifted = per && b.posw && sp.g[0] >= 3 && sp.g[1] >= 3 && (DIM == 2 || sp.g[2] >= 3);
-  const float4* __restrict__ P = shifted ? b.posw : b.pos[ld_cg_u32(&b.ctl->pos_sel)];
+  const float4* __restrict__ P = shifted ? b.posw : b.pos[ld_nc_u32(&b.ctl->pos_sel)];
   const float4 pi = P[t];
   const float skin = b.nl_skin;
   const int cap = b.nl_cap;
@@ -572,8 +572,8 @@ template <int DIM, bool GENERAL, int LAW, int G>
 __global__ void __launch_bounds__(128) k_force_small(Bufs b, int mode) {
   const long long t = (blockIdx.x * 128LL + threadIdx.x) / G;
   const int lane = threadIdx.x & 31, g = lane % G, base = lane - g;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  const bool use_list = b.nl_cap > 0 && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
+  const bool use_list = b.nl_cap > 0 && (ld_nc_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
   float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
   float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t tg = 0u;
@@ -682,7 +682,7 @@ template <int DIM>
 __global__ void k_energy(Bufs b, double* __restrict__ out) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   double e_pair = 0.0, e_grav = 0.0, e_kin = 0.0;
   const float4* __restrict__ P = b.pos[ps];
   float4 pi = P[t];
@@ -794,7 +794,7 @@ __global__ void k_contacts(Bufs b, int pass, int32_t* __restrict__ counts,
                            long long cap) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+  unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   const float4* __restrict__ P = b.pos[ps];
   float4 pi = P[t];
   uint32_t tg = b.tag[sel][t];

@@ -43,8 +43,8 @@ template <int DIM, int LAW>
 __global__ void k_rb_force(Bufs b) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
-  const bool use_list = b.nl_cap > 0 && (ld_cg_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
+  const bool use_list = b.nl_cap > 0 && (ld_nc_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
   const float4* __restrict__ P = b.pos[ps];
   const float4 pi = P[t];
   const uint32_t tg = b.tag[sel][t];
@@ -376,7 +376,7 @@ __global__ void k_rb_place(Bufs b, int in_place) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   float d2 = 0.0f;
   if (t < b.P) {
-    const unsigned int sel = ld_cg_u32(&b.ctl->sel), ps = ld_cg_u32(&b.ctl->pos_sel);
+    const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
     const float4 old = b.pos[ps][t];
     const long long i = b.orig[sel][t];
     const int c = b.sclump[i];

@@ -173,7 +173,7 @@ __device__ __forceinline__ int last_le(const int* a, int lo, int hi, int v) {
 
 template <int DIM>
 __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
-  if (ld_cg_u32(&b.ctl->nl_dirty) == 0u) return;
+  if (ld_nc_u32(&b.ctl->nl_dirty) == 0u) return;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_hrow[kMaxHomeRows + 1];
   __shared__ int s_scan[32];
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
   const int NV = bk.VX * bk.VY * bk.VZ, HD = bk.H * bk.D, nrows = bk.VY * bk.VZ;
   const float skin = b.nl_skin, eps = sp.nl_eps;
   const int32_t* __restrict__ cs = b.cell_start;
-  const unsigned int sel = ld_cg_u32(&b.ctl->sel);
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel);
   bool direct = (td.flags & TILE_DIRECT) != 0 || NV > NVC || nrows > NR;
 
   if (!direct) {
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
     }
     __syncthreads();
     const int cnt = tile_scan_inplace(s_hrow, HD, s_scan);
-    const float4* __restrict__ Pc = b.pos[ld_cg_u32(&b.ctl->pos_sel)];
+    const float4* __restrict__ Pc = b.pos[ld_nc_u32(&b.ctl->pos_sel)];
     const uint32_t mark = per ? 0x80000000u : 0u;
     for (int h = threadIdx.x; h < cnt; h += TB) {
       const int r = last_le(s_hrow, 0, HD, h);
