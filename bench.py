@@ -187,19 +187,25 @@ def run_reference(args, rank, world):
 
 
 # -------------------------------------------------------------- ours
-def traffic_from_profile(workload, n, skin):
-    """dram bytes per fused-kernel launch from the committed ncu summary, when it
-    was captured on this workload's size and skin; else None."""
-    p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"  # written from an ncu capture
-    if p.exists():
-        try:
-            d = json.loads(p.read_text())
-            if d.get("n") != n or abs(float(d.get("skin", -1.0)) - float(skin)) > 1e-3:
-                return None
-            return d.get("dram_bytes_per_launch")
-        except Exception:
-            return None
-    return None
+def traffic_from_profile(workload, n, skin, pruning, prune_frac):
+    """DRAM bytes per fused-kernel launch from the committed ncu captures
+    (profiles/k_force_<workload>_traffic.json), when one was taken on this workload's
+    size, skin (within 5 %) and pruning setting: the inner- and prune-pass figures
+    weighted by the fraction of prune passes.  Returns (bytes, capture) or (None, None)."""
+    p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"
+    try:
+        d = json.loads(p.read_text())
+    except Exception:
+        return None, None
+    if d.get("n") != n:
+        return None, None
+    for c in d.get("captures", []):
+        if abs(float(c["skin"]) - float(skin)) > 0.05 * float(skin) or bool(c["pruning"]) != bool(pruning):
+            continue
+        if pruning:
+            return prune_frac * c["prune_pass_bytes"] + (1.0 - prune_frac) * c["inner_pass_bytes"], c
+        return c["full_pass_bytes"], c
+    return None, None
 
 
 def peaks():
@@ -289,12 +295,15 @@ def run_ours(args, rank, world, dist):
     graphs_captured_timed = stats["graphs"] - graphs_before
 
     # instrumented pass: per-launch events around the fused force kernel
+    prunes0 = eng.stats()["prunes"]
     tot_ms, force_ms = eng.step_timed(CHUNK)
+    prune_frac = (eng.stats()["prunes"] - prunes0) / CHUNK
     force_avg_ms = force_ms / CHUNK
     B = BYTES_PER_PARTICLE_STEP[w.dim]
     peak, peak_kind = peaks()
     achieved = B * w.N / (force_avg_ms * 1e-3) / 1e9
-    traffic = traffic_from_profile(args.workload, w.N, skin)
+    pruning = stats["prunes"] > 0
+    traffic, capture = traffic_from_profile(args.workload, w.N, skin, pruning, prune_frac)
 
     # Secondary figures: the whole step against the same roofline; the step with the re-sort
     # traffic counted (a re-sort reads and writes each slot's record: position and velocity
@@ -376,6 +385,10 @@ def run_ours(args, rank, world, dist):
                                    "regrowths": stats["list_regrowths"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "traffic_source": (f"ncu capture at skin {capture['skin']}, pruning "
+                                        f"{'on' if capture['pruning'] else 'off'}, weighted by this pass's "
+                                        f"prune fraction {prune_frac:.2f} ({capture['source']})")
+                     if capture else "no ncu capture at this skin and pruning setting",
                      "kernel": ("k_force_small (8 lanes a slot), timed per launch: the timed region runs the "
                                 "same step inside cooperative many-step launches (k_multi)")
                      if stats.get("many_step") else "k_force (fused force + integrate)",
