@@ -4,8 +4,10 @@ JAX cannot be installed here, so this script runs the reference's source tree on
 stand-in for the JAX API in ``tests/golden/jaxshim`` (see its README.txt): the reference's
 State.create, System.create, System.step (``jaxdem/system.py:60-82, 701-748``), the cell-list
 collider (``jaxdem/colliders/cell_list.py``), the spring / Hertz laws, the Verlet, Euler,
-VV-spiral and spiral integrators, the periodic / reflect / free domains, the thermal energies
-and ``create_neighbor_list`` execute as written, with jax.numpy evaluated by numpy.
+VV-spiral and spiral integrators, the Cundall-Strack law with "elasticfrict" materials, rigid
+clumps (per-clump force / torque sums and the reflect domain's clump collisions), the periodic /
+reflect / free domains, the thermal energies and ``create_neighbor_list`` execute as written,
+with jax.numpy evaluated by numpy.
 
 Every input is drawn here with numpy's PCG64 and stored beside the outputs, so the fixtures
 are self-contained:
@@ -30,39 +32,71 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 
-# name: dim, N, domain, radii ("bi" 0.5/0.7, "poly" U[0.4, 0.6], "mono" 0.5), packing fraction,
-# velocity sigma, dt, gravity, restitution, linear / rotation integrator, force law, young moduli
-# of the materials, strides between recorded snapshots, neighbour-list cutoff factor
+# name: PCG64 seed, dim, N (spheres, or clumps for radii "clump"), domain, radii ("bi" 0.5/0.7,
+# "poly" U[0.4, 0.6], "mono" 0.5, "clump" U[0.4, 0.5]), packing fraction, velocity and spin sigmas,
+# dt, gravity, restitution, linear / rotation integrator, force law, the materials' young moduli
+# (and poisson / e / mu / mu_r for Cundall-Strack), strides between recorded snapshots,
+# neighbour-list cutoff factor
 CASES = {
-    "per3d_bi": dict(dim=3, N=96, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4, strides=[1, 9, 20],
+    "per3d_bi": dict(seed=1005, dim=3, N=96, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4, strides=[1, 9, 20],
                      nl=3.0),
-    "per2d_poly": dict(dim=2, N=96, domain="periodic", radii="poly", phi=0.7, vsig=0.1, dt=5e-4,
+    "per2d_poly": dict(seed=1004, dim=2, N=96, domain="periodic", radii="poly", phi=0.7, vsig=0.1, dt=5e-4,
                        strides=[1, 9, 20], nl=2.5),
-    "refl2d_grav": dict(dim=2, N=80, domain="reflect", radii="poly", phi=0.5, vsig=0.5, dt=1e-3,
+    "refl2d_grav": dict(seed=1006, dim=2, N=80, domain="reflect", radii="poly", phi=0.5, vsig=0.5, dt=1e-3,
                         gravity=[0.0, -1.0], strides=[1, 9, 30]),
-    "refl3d_e08": dict(dim=3, N=64, domain="reflect", radii="bi", phi=0.35, vsig=0.8, dt=1e-3,
+    "refl3d_e08": dict(seed=1007, dim=3, N=64, domain="reflect", radii="bi", phi=0.35, vsig=0.8, dt=1e-3,
                        gravity=[0.0, 0.0, -2.0], restitution=0.8, strides=[1, 9, 30]),
-    "free3d": dict(dim=3, N=64, domain="free", radii="bi", phi=0.45, vsig=0.2, dt=5e-4, strides=[1, 9, 20]),
-    "rot3d_vvspiral": dict(dim=3, N=64, domain="periodic", radii="mono", phi=0.45, vsig=0.1, dt=1e-3,
+    "free3d": dict(seed=1001, dim=3, N=64, domain="free", radii="bi", phi=0.45, vsig=0.2, dt=5e-4, strides=[1, 9, 20]),
+    "rot3d_vvspiral": dict(seed=1009, dim=3, N=64, domain="periodic", radii="mono", phi=0.45, vsig=0.1, dt=1e-3,
                            wsig=2.0, rotation="verletspiral", strides=[1, 9, 10]),
-    "rot2d_spiral": dict(dim=2, N=64, domain="periodic", radii="mono", phi=0.6, vsig=0.1, dt=1e-3,
+    "rot2d_spiral": dict(seed=1008, dim=2, N=64, domain="periodic", radii="mono", phi=0.6, vsig=0.1, dt=1e-3,
                          wsig=2.0, rotation="spiral", strides=[1, 9, 10]),
-    "hertz3d": dict(dim=3, N=64, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4, law="hertz",
+    "hertz3d": dict(seed=1002, dim=3, N=64, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4, law="hertz",
                     strides=[1, 9, 10]),
-    "mat2_3d": dict(dim=3, N=64, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4,
+    "mat2_3d": dict(seed=1003, dim=3, N=64, domain="periodic", radii="bi", phi=0.5, vsig=0.1, dt=5e-4,
                     young=[1.0e3, 3.0e3], strides=[1, 9, 10]),
-    "euler2d": dict(dim=2, N=64, domain="periodic", radii="poly", phi=0.6, vsig=0.1, dt=5e-4, linear="euler",
+    "euler2d": dict(seed=1000, dim=2, N=64, domain="periodic", radii="poly", phi=0.6, vsig=0.1, dt=5e-4, linear="euler",
                     strides=[1, 9, 10]),
-    "tiny3d": dict(dim=3, N=12, domain="periodic", radii="mono", box=2.6, vsig=0.2, dt=1e-3, strides=[1, 9, 20]),
+    "tiny3d": dict(seed=1010, dim=3, N=12, domain="periodic", radii="mono", box=2.6, vsig=0.2, dt=1e-3, strides=[1, 9, 20]),
+    # Cundall-Strack with two "elasticfrict" materials, random spins (rolling friction active)
+    "cs3d": dict(seed=1011, dim=3, N=64, domain="periodic", radii="bi", phi=0.5, vsig=0.3, dt=5e-4, wsig=2.0,
+                 law="cundallstrack", strides=[1, 9, 10], young=[1.0e3, 3.0e3], poisson=[0.25, 0.3], e=[0.6, 0.8],
+                 mu=[0.4, 0.3], mu_r=[0.05, 0.1]),
+    "cs2d_refl": dict(seed=1012, dim=2, N=64, domain="reflect", radii="poly", phi=0.55, vsig=0.5, dt=5e-4, wsig=2.0,
+                      gravity=[0.0, -1.0], law="cundallstrack", rotation="spiral", strides=[1, 9, 20],
+                      young=[1.0e3, 2.0e3], poisson=[0.3, 0.2], e=[0.5, 0.9], mu=[0.5, 0.2], mu_r=[0.0, 0.2]),
+    # rigid clumps of one to three spheres (State.create with pos_p, q, clump_id, mass, inertia)
+    "clump3d": dict(seed=1013, dim=3, N=40, domain="periodic", radii="clump", phi=0.35, vsig=0.3, dt=1e-3, wsig=1.0,
+                    strides=[1, 9, 20]),
+    "clump2d_refl": dict(seed=1014, dim=2, N=40, domain="reflect", radii="clump", phi=0.3, vsig=0.5, dt=1e-3,
+                         wsig=1.0, gravity=[0.0, -2.0], strides=[1, 9, 30]),
 }
 X64_CASES = ["per3d_bi", "refl2d_grav"]
 
 
+def _clumps(rng, n_clumps, dim):
+    """Clumps of one to three spheres (radius U[0.4, 0.5]): per-member body-frame offsets,
+    the clump index of each member, and per-clump random orientations (w, x, y, z)."""
+    sizes = rng.choice([1, 2, 3], n_clumps, p=[0.2, 0.5, 0.3])
+    offs = {1: [[0.0, 0.0, 0.0]], 2: [[-0.35, 0.0, 0.0], [0.35, 0.0, 0.0]],
+            3: [[-0.3, -0.2, 0.0], [0.3, -0.2, 0.0], [0.0, 0.35, 0.0]]}
+    pos_p = np.concatenate([np.asarray(offs[s])[:, :dim] for s in sizes])
+    cid = np.repeat(np.arange(n_clumps), sizes)
+    if dim == 2:
+        a = rng.uniform(0, 2 * np.pi, n_clumps)
+        q = np.stack([np.cos(a / 2), 0 * a, 0 * a, np.sin(a / 2)], 1)
+    else:
+        q = rng.normal(size=(n_clumps, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return pos_p, cid, q
+
+
 def make_inputs(name, c):
     """Seeded inputs of one case (numpy PCG64)."""
-    seed = 1000 + sorted(CASES).index(name)
-    rng = np.random.Generator(np.random.PCG64(seed))
+    rng = np.random.Generator(np.random.PCG64(c["seed"]))
     N, dim = c["N"], c["dim"]
+    if c["radii"] == "clump":
+        return _clump_inputs(rng, c)
     if c["radii"] == "bi":
         rad = rng.choice([0.5, 0.7], size=N)
     elif c["radii"] == "poly":
@@ -85,17 +119,56 @@ def make_inputs(name, c):
                 mat_id=mat.astype(np.int32), box=np.full(dim, L, np.float32), anchor=np.zeros(dim, np.float32))
 
 
+def _clump_inputs(rng, c):
+    """A clump case: ``N`` clumps; members carry their clump's centre, velocity, spin,
+    orientation, mass (the members' volumes at density 1) and principal inertia."""
+    dim, nc = c["dim"], c["N"]
+    pos_p, cid, qc = _clumps(rng, nc, dim)
+    N = len(cid)
+    rad = rng.uniform(0.4, 0.5, N).astype(np.float32)
+    vol = (np.pi * rad.astype(np.float64) ** 2) if dim == 2 else (4.0 / 3.0 * np.pi * rad.astype(np.float64) ** 3)
+    L = float((vol.sum() / c["phi"]) ** (1.0 / dim))
+    lo, hi = (1.0, L - 1.0) if c["domain"] == "reflect" else (0.0, L)
+    centres = rng.uniform(lo, hi, (nc, dim))
+    vc = rng.normal(0.0, c["vsig"], (nc, dim))
+    ad = 3 if dim == 3 else 1
+    wc = rng.normal(0.0, c["wsig"], (nc, ad))
+    Mc = np.bincount(cid, weights=vol)
+    Ic = np.stack([Mc * (0.2 + 0.05 * a) for a in range(ad)], 1)
+    f = np.float32
+    return dict(pos=centres[cid].astype(f), vel=vc[cid].astype(f), rad=rad, ang_vel=wc[cid].astype(f),
+                mat_id=np.zeros(N, np.int32), box=np.full(dim, L, f), anchor=np.zeros(dim, f),
+                pos_p=pos_p.astype(f), q=qc[cid].astype(f), clump_id=cid.astype(np.int32), mass_in=Mc[cid].astype(f),
+                inertia_in=Ic[cid].astype(f))
+
+
+def _materials(jd, c):
+    """The case's materials: "elastic" (young, Poisson 0.3), or "elasticfrict" with the
+    case's poisson / e / mu / mu_r lists for the Cundall-Strack law."""
+    youngs = c.get("young", [1.0e3])
+    if c.get("law") == "cundallstrack":
+        return [jd.Material.create("elasticfrict", density=1.0, young=float(y), poisson=float(p), mu=float(mu),
+                                   e=float(e), mu_r=float(mr))
+                for y, p, e, mu, mr in zip(youngs, c["poisson"], c["e"], c["mu"], c["mu_r"])]
+    return [jd.Material.create("elastic", density=1.0, young=float(y), poisson=0.3) for y in youngs]
+
+
 def run_case(jd, name, c, x64):
     import jax.numpy as jnp
 
     inp = make_inputs(name, c)
     dim = c["dim"]
-    youngs = c.get("young", [1.0e3])
-    mats = [jd.Material.create("elastic", density=1.0, young=float(y), poisson=0.3) for y in youngs]
-    mat_table = jd.MaterialTable.from_materials(mats)
+    mat_table = jd.MaterialTable.from_materials(_materials(jd, c))
     fdt = np.float64 if x64 else np.float32
-    state = jd.State.create(pos=inp["pos"].astype(fdt), vel=inp["vel"].astype(fdt), rad=inp["rad"].astype(fdt),
-                            ang_vel=inp["ang_vel"].astype(fdt), mat_id=inp["mat_id"], mat_table=mat_table)
+    if "clump_id" in inp:
+        state = jd.State.create(pos=inp["pos"].astype(fdt), pos_p=inp["pos_p"].astype(fdt), q=inp["q"].astype(fdt),
+                                vel=inp["vel"].astype(fdt), rad=inp["rad"].astype(fdt),
+                                ang_vel=inp["ang_vel"].astype(fdt), mass=inp.pop("mass_in").astype(fdt),
+                                inertia=inp.pop("inertia_in").astype(fdt), clump_id=inp["clump_id"],
+                                mat_id=inp["mat_id"])
+    else:
+        state = jd.State.create(pos=inp["pos"].astype(fdt), vel=inp["vel"].astype(fdt), rad=inp["rad"].astype(fdt),
+                                ang_vel=inp["ang_vel"].astype(fdt), mat_id=inp["mat_id"], mat_table=mat_table)
     domain_kw = {"box_size": tuple(float(x) for x in inp["box"]), "anchor": tuple(float(x) for x in inp["anchor"])}
     if c["domain"] == "reflect":
         domain_kw["restitution_coefficient"] = float(c.get("restitution", 1.0))

@@ -83,14 +83,26 @@ def reference_osystem(d, dtype=np.float32):
     young = np.asarray(d["young_eff"], dtype)
     if law == "hertz":
         young = R.hertz_constant(np.asarray(m.get("young", [1.0e3])), np.full(len(m.get("young", [1.0e3])), 0.3))
+    props = None
+    if law == "cundallstrack":
+        young, props = reference_cs_tables(d)
     grav = np.zeros(dim, dtype) if not m.get("gravity") else np.asarray(m["gravity"], dtype)
     return R.OSystem(dim=dim, domain=m["domain"], box_size=np.asarray(d["box"], dtype).copy(),
                      anchor=np.asarray(d["anchor"], dtype).copy(), young_eff=np.asarray(young, dtype),
                      dt=dtype(m["dt"]), cell_size=dtype(d["cell_size"]), neighbor_mask=mask, gravity=grav,
                      restitution=dtype(m.get("restitution", 1.0)), linear=m.get("linear", "verlet"),
-                     rotation=m.get("rotation", "verletspiral"), force_law=law)
+                     rotation=m.get("rotation", "verletspiral"), force_law=law,
+                     mat_props=None if props is None else np.asarray(props, dtype))
+
+
+def reference_cs_tables(d):
+    """The Cundall-Strack tables of a golden case: the damping ratio beta (M, M) and the
+    per-material (young, shear modulus, mu, mu_r) rows, from the case's material lists."""
+    m = d["meta"]
+    return R.cs_tables(young=m["young"], poisson=m["poisson"], e=m["e"], mu=m["mu"], mu_r=m["mu_r"])
 
 
 def reference_ostate(d, dtype=np.float32):
+    clump = {k: d[k] for k in ("pos_p", "q", "clump_id") if k in d}
     return R.make_state(d["pos"], vel=d["vel"], rad=d["rad"], mass=d["mass"], mat_id=d["mat_id"],
-                        ang_vel=d["ang_vel"], inertia=d["inertia"], dtype=dtype)
+                        ang_vel=d["ang_vel"], inertia=d["inertia"], dtype=dtype, **clump)

@@ -11,8 +11,18 @@ float64 cases (jax_enable_x64) pin the oracle's float64 build.
 
 Cases: 3D bidisperse periodic, 2D polydisperse periodic, 2D reflect with gravity, 3D
 reflect with restitution 0.8 and gravity, 3D free domain, VV-spiral and spiral rotation
-with random spins, Hertz law, two materials, direct Euler, and a periodic box of two cells
-per axis (the reference de-duplicates the stencil).
+with random spins, Hertz law, two materials, direct Euler, a periodic box of two cells
+per axis (the reference de-duplicates the stencil), Cundall-Strack with two "elasticfrict"
+materials and rolling friction (3D periodic; 2D reflect with gravity and the spiral
+integrator), and rigid clumps of one to three spheres (3D periodic; 2D reflect with gravity).
+
+One reduction is not bit-reproducible by construction: the reference sums each particle's
+per-stencil-cell accumulators with ``x.sum(axis=0)`` (``colliders/cell_list.py:255-256``),
+whose order XLA leaves unspecified.  On the numpy stand-in that sum is pairwise over the
+contiguous (9, 1) torque block of a 2D particle (numpy's 8-way blocked summation), where the
+oracle adds the nine cells left to right.  Only 2D torques that are non-zero and spread over
+at least eight cells see it (the 2D Cundall-Strack case): there the torque, the angular
+velocity and the orientation are held to a few float32 ulps, everything else bit for bit.
 """
 
 from __future__ import annotations
@@ -30,16 +40,29 @@ X64_CASES = ["per3d_bi", "refl2d_grav"]
 
 
 def test_fixture_set_is_complete():
-    assert len(CASES) >= 11, CASES
+    assert len(CASES) >= 15, CASES
+    laws = {load_reference_case(c)["meta"].get("law", "spring") for c in CASES}
+    assert laws == {"spring", "hertz", "cundallstrack"}
+    assert sum("clump_id" in load_reference_case(c) for c in CASES) >= 2
+
+
+def _torque_order_free(d):
+    """2D cases with pair torques: the stencil-cell sum order of the torque is unspecified."""
+    return d["meta"]["dim"] == 2 and d["meta"].get("law") == "cundallstrack"
+
+
+def _same(a, b, loose, rtol=1e-6, atol=0.0):
+    return np.allclose(a, b, rtol=rtol, atol=atol) if loose else np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("name", CASES)
 def test_numpy_oracle_reproduces_reference_bit_for_bit(name):
     d = load_reference_case(name)
+    loose = _torque_order_free(d)
     sy, st = reference_osystem(d), reference_ostate(d)
     f0, t0 = R.cell_list_force(st, sy)
     assert np.array_equal(f0, d["force0"]), f"{name}: compute_force differs (err {force_err(f0, d['force0'])})"
-    assert np.array_equal(t0, d["torque0"])
+    assert _same(t0, d["torque0"], loose, atol=1e-6 * np.abs(d["torque0"]).max())
     e = R.compute_energy(st, sy)
     # thermal.compute_potential_energy: force-manager (gravity) PE + collider PE
     assert np.isclose(e[0] + e[1], d["pe0"], rtol=1e-6, atol=1e-6)
@@ -53,8 +76,9 @@ def test_numpy_oracle_reproduces_reference_bit_for_bit(name):
             f"{name} after {n} steps: positions differ by {min_image_diff(s.pos_c, d['snap_pos'][i], box)}")
         assert np.array_equal(s.vel, d["snap_vel"][i])
         assert np.array_equal(s.force, d["snap_force"][i])
-        assert np.array_equal(s.q, d["snap_q"][i])
-        assert np.array_equal(s.ang_vel, d["snap_ang_vel"][i])
+        assert _same(s.q, d["snap_q"][i], loose, rtol=0.0, atol=1e-7)
+        assert _same(s.ang_vel, d["snap_ang_vel"][i], loose, atol=1e-6)
+        assert _same(s.torque, d["snap_torque"][i], loose, atol=1e-6 * np.abs(d["snap_torque"][i]).max())
         if d["meta"]["domain"] == "free":
             assert np.array_equal(sy.box_size, d["snap_box"][i])
             assert np.array_equal(sy.anchor, d["snap_anchor"][i])
@@ -69,8 +93,13 @@ def test_neighbor_list_reproduces_reference(name):
     assert np.array_equal(nl, d["nl"])
 
 
-C_CASES = [c for c in CASES if not load_reference_case(c)["meta"].get("rotation") or
-           not np.any(load_reference_case(c)["ang_vel"])]
+def _c_covers(d):
+    """The C restatement covers smooth spheres under the spring and Hertz laws."""
+    return (not np.any(d["ang_vel"]) and "clump_id" not in d
+            and d["meta"].get("law", "spring") in ("spring", "hertz"))
+
+
+C_CASES = [c for c in CASES if _c_covers(load_reference_case(c))]
 
 
 @pytest.mark.parametrize("name", C_CASES)
