@@ -2,9 +2,11 @@
 (tests/golden/reference_<case>.npz; see tests/golden/make_reference_golden.py).
 
 Bars of the benchmark specification: forces within 1e-5 floored relative error of the
-reference's float32 compute_force; positions within 1e-4 after each recorded stride of
-System.step; rotation state (q, ang_vel) for the VV-spiral and spiral integrators; the
-reference's create_neighbor_list bit for bit; energies within 1e-5.  Against the float64
+reference's float32 compute_force (torques within 1e-5 of the largest torque); positions
+within 1e-4 after each recorded stride of System.step; rotation state (q, ang_vel) for the
+VV-spiral and spiral integrators; the reference's create_neighbor_list bit for bit; energies
+within 1e-5.  The cases include the Cundall-Strack law (rolling friction, two materials) and
+rigid clumps, in periodic and reflecting boxes.  Against the float64
 (jax_enable_x64) runs the float32 engine's error is stated and bounded.
 """
 
@@ -35,12 +37,20 @@ def _engine(d):
                 restitution=m.get("restitution", 1.0), gravity=sy.gravity, cell_size=float(d["cell_size"]),
                 search_range=1)
     return Engine(m["dim"], [desc], sy.young_eff, skin=0.1 * float(d["rad"].max()),
-                  force_law=m.get("law", "spring"))
+                  force_law=m.get("law", "spring"), material_props=sy.mat_props)
 
 
 def _upload(eng, d):
+    clump = {k: d[k] for k in ("pos_p", "q", "clump_id") if k in d}
     eng.upload(pos=d["pos"], vel=d["vel"], rad=d["rad"], mass=d["mass"], mat_id=d["mat_id"], ang_vel=d["ang_vel"],
-               inertia=d["inertia"])
+               inertia=d["inertia"], **clump)
+
+
+def _torque_err(t, ref):
+    """Largest torque error over the largest reference torque (torques are zero for
+    smooth spheres under the central spring and Hertz laws)."""
+    scale = max(float(np.abs(ref).max()), 1e-30)
+    return float(np.abs(t - ref).max()) / scale
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -52,7 +62,8 @@ def test_engine_matches_reference_outputs(name):
         _upload(eng, d)
         e0 = eng.energy()
         eng.compute_force()
-        f0 = eng.download()["force"]
+        out0 = eng.download()
+        f0 = out0["force"]
         _upload(eng, d)
         prev, snaps = 0, []
         for n in d["snap_steps"]:
@@ -67,6 +78,7 @@ def test_engine_matches_reference_outputs(name):
         eng.close()
     assert force_err(f0, d["force0"]) <= 1e-5, f"{name}: compute_force err {force_err(f0, d['force0'])}"
     assert global_force_err(f0, d["force0"]) <= 1e-5
+    assert _torque_err(out0["torque"], d["torque0"]) <= 1e-5, f"{name}: torque err"
     # thermal.compute_potential_energy: force-manager (gravity) PE + collider PE
     assert np.allclose(e0[0] + e0[1], d["pe0"], rtol=1e-5, atol=1e-5), (e0, d["pe0"])
     assert np.allclose(e0[2], d["ke0"], rtol=1e-5, atol=1e-6)
@@ -78,6 +90,7 @@ def test_engine_matches_reference_outputs(name):
         assert force_err(out["force"], d["snap_force"][i]) <= 1e-4
         assert np.allclose(out["q"], d["snap_q"][i], atol=2e-6), f"{name}: q after {n} steps"
         assert np.allclose(out["ang_vel"], d["snap_ang_vel"][i], rtol=1e-5, atol=1e-5)
+        assert _torque_err(out["torque"], d["snap_torque"][i]) <= 1e-4, f"{name}: torque after {n} steps"
     if nl is not None:
         assert ovf == bool(d["nl_overflow"])
         assert np.array_equal(nl, d["nl"])
