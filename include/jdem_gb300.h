@@ -120,7 +120,11 @@ typedef struct {
  * Rigid clumps (State.add_clump, state.py:1230-1420): pos_p (N, dim) holds each
  * sphere's body-frame offset and clump_id (N) the clump index within its
  * system; members store their clump's pos_c, vel, q, ang_vel, mass and
- * inertia.  NULL for both means every sphere is its own body. */
+ * inertia.  NULL for both means every sphere is its own body.  Clumps take
+ * every force law: a Cundall-Strack contact of a member uses its clump's
+ * velocity, angular velocity and mass, with the contact arm from the sphere's
+ * own centre (cundall_strack.py:126-176), and jdem_neighbor_list lists the
+ * members' world positions without same-clump pairs. */
 typedef struct {
   float* pos_c;
   float* vel;

@@ -44,6 +44,8 @@ void launch_rb_init(int dim, const Bufs& b, const float* pos, const float* vel, 
 void launch_rb_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc, float4* q, float* angv,
                       float* torque, bool per_sphere, cudaStream_t st);
 void launch_rb_energy(int dim, const Bufs& b, double* out, cudaStream_t st);
+// members' world positions pos_c + R(q) pos_p, caller order (pos: P x dim)
+void launch_rb_world(int dim, const Bufs& b, float* pos, cudaStream_t st);
 void launch_nlbuild(int dim, const Bufs& b, cudaStream_t st);
 // brick list build (jdem_tiles.cu)
 size_t tbuild_smem(int nst, int nv, int nrows);

@@ -107,8 +107,8 @@ template <int DIM>
 __global__ void k_nl_build(long long P, const float* __restrict__ pos, const int32_t* __restrict__ sys_of,
                            const NlGrid* __restrict__ grids, const int32_t* __restrict__ start,
                            const int32_t* __restrict__ perm, const int32_t* __restrict__ bond, int bond_w,
-                           int interact_same_bond, float cutoff_sq, int max_nb, int32_t* __restrict__ out,
-                           unsigned int* __restrict__ overflow) {
+                           int interact_same_bond, const int32_t* __restrict__ body, float cutoff_sq, int max_nb,
+                           int32_t* __restrict__ out, unsigned int* __restrict__ overflow) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= P) return;
   const NlGrid& G = grids[sys_of[i]];
@@ -135,7 +135,8 @@ __global__ void k_nl_build(long long P, const float* __restrict__ pos, const int
     int local = 0;
     for (int k = start[cell]; k < start[cell + 1]; ++k) {
       int j = perm[k];
-      if (j == (int)i) continue;  // same clump (valid_interaction_mask)
+      // same body (valid_interaction_mask): a sphere, or a rigid clump's members
+      if (body ? body[j] == body[i] : j == (int)i) continue;
       if (bond_w > 0 && !interact_same_bond) {
         bool bonded = false;
         for (int w = 0; w < bond_w; ++w) bonded |= bond[(long long)j * bond_w + w] == (int)i;
@@ -171,7 +172,6 @@ int JdemHandle::neighbor_list(float cutoff, int max_nb, int32_t* out, int32_t* o
   if (overflow) *overflow = 0;
   if (P == 0 || max_nb == 0) return JDEM_OK;
   if (!out) return fail(JDEM_ERR_BAD_ARG, "neighbor_list: null output");
-  if (b.NC) return fail(JDEM_ERR_UNSUPPORTED, "neighbor_list: rigid clumps are not supported");
   cudaSetDevice(dev);
   // Reference grid per system.
   std::vector<NlGrid> grids((size_t)S);
@@ -230,8 +230,9 @@ int JdemHandle::neighbor_list(float cutoff, int max_nb, int32_t* out, int32_t* o
     cleanup();
     return rc;
   }
-  // positions in caller order
-  launch_unpack(dim, b, st_pos, st_vel, st_frc, stream);
+  // positions in caller order: state.pos, the members' world positions for clumps
+  if (b.NC) launch_rb_world(dim, b, st_pos, stream);
+  else launch_unpack(dim, b, st_pos, st_vel, st_frc, stream);
   cudaMemcpyAsync(d_grids, grids.data(), sizeof(NlGrid) * S, cudaMemcpyHostToDevice, stream);
   cudaMemsetAsync(d_cnt, 0, 4 * (size_t)c_total, stream);
   cudaMemsetAsync(d_out, 0xFF, 4 * (size_t)P * max_nb, stream);
@@ -256,10 +257,12 @@ int JdemHandle::neighbor_list(float cutoff, int max_nb, int32_t* out, int32_t* o
   float cutoff_sq = cutoff * cutoff;
   if (dim == 3)
     k_nl_build<3><<<pb, 256, 0, stream>>>(P, st_pos, st_sys, d_grids, d_start, d_perm, d_bond, bond_w,
-                                          interact_same_bond, cutoff_sq, max_nb, d_out, d_ovf);
+                                          interact_same_bond, b.NC ? b.sclump : nullptr, cutoff_sq, max_nb, d_out,
+                                          d_ovf);
   else
     k_nl_build<2><<<pb, 256, 0, stream>>>(P, st_pos, st_sys, d_grids, d_start, d_perm, d_bond, bond_w,
-                                          interact_same_bond, cutoff_sq, max_nb, d_out, d_ovf);
+                                          interact_same_bond, b.NC ? b.sclump : nullptr, cutoff_sq, max_nb, d_out,
+                                          d_ovf);
   cudaError_t e = cudaGetLastError();
   unsigned int h_ovf = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, 4 * (size_t)P * max_nb, cudaMemcpyDeviceToHost, stream);

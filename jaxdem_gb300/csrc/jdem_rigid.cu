@@ -9,6 +9,8 @@
 //   k_rb_force   per sphere: contact force from the list (spheres of one clump
 //                excluded, colliders/__init__.py:225-243) and its torque about
 //                the clump centre, cross(R(q) pos_p, F) (cell_list.py:452-464);
+//                k_rb_cs_force for Cundall-Strack contacts, whose pair torques
+//                are added to that;
 //   k_rb_clump   per clump: ForceManager.apply -- F_contact + gravity * (M /
 //                count) summed over the members, torques summed
 //                (force_manager.py:338-425) -- then the integrators'
@@ -18,6 +20,7 @@
 // Members are summed in caller order.  Periodic, free and reflect domains
 // (the reflect domain's clump impulses: clump_reflect).
 #include "jdem_device.cuh"
+#include "jdem_cs.cuh"
 #include "jdem_kernels.h"
 #include "jdem_pair.cuh"
 #include "jdem_rot.cuh"
@@ -78,6 +81,78 @@ __global__ void k_rb_force(Bufs b) {
   }
   b.sf[i] = make_float4(F[0], F[1], F[2], 0.0f);
   b.stq[i] = T;
+}
+
+// Cundall-Strack contacts of every sphere (cundall_strack.py:100-196).  A
+// member's velocity, angular velocity and mass are its clump's (every member
+// stores the clump's values), and the contact arm runs from the sphere's own
+// centre; the sphere's torque about the clump centre is the sum of the pair
+// torques plus cross(R(q) pos_p, F) (cell_list.py:452-464).
+template <int DIM>
+__global__ void k_rb_cs_force(Bufs b) {
+  constexpr int AD = DIM == 3 ? 3 : 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
+  const bool use_list = b.nl_cap > 0 && (ld_nc_u32(&b.ctl->status) & ST_NL_OVERFLOW) == 0u;
+  const float4* __restrict__ P = b.pos[ps];
+  const float4 pi = P[t];
+  const uint32_t tg = b.tag[sel][t];
+  const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
+  const bool per = sp.domain == DOM_PERIODIC;
+  const int mi = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+  const long long oi = b.orig[sel][t];
+  const int ci = b.sclump[oi];
+  const float4 vi4 = b.cvel[ci], wi4 = b.cw[ci];
+  const float Mi = b.cpos[ci].w;
+  const float vi[3] = {vi4.x, vi4.y, vi4.z}, wi[3] = {wi4.x, wi4.y, wi4.z};
+  float F[3] = {0, 0, 0}, eF[3] = {0, 0, 0}, T[3] = {0, 0, 0}, eT[3] = {0, 0, 0};
+  auto visit = [&](int j, bool may_wrap) {
+    const float4 pj = P[j];
+    float d[3];
+    const float dsq = pair_disp<DIM>(sp, per && may_wrap, pi, pj, d[0], d[1], d[2]);
+    const float R = pi.w + pj.w;
+    if (!(dsq < R * R * 1.000001f)) return;
+    const int oj = b.orig[sel][j];
+    const int cj = b.sclump[oj];
+    if (cj == ci) return;  // one body (valid_interaction_mask)
+    if (b.bond_w > 0 && !b.interact_same_bond) {
+      bool bonded = false;
+      for (int w = 0; w < b.bond_w; ++w) bonded |= (b.bond[oi * b.bond_w + w] == oj);
+      if (bonded) return;
+    }
+    const int mj = (b.tag[sel][j] >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
+    const float4 vj4 = b.cvel[cj], wj4 = b.cw[cj];
+    const float vj[3] = {vj4.x, vj4.y, vj4.z}, wj[3] = {wj4.x, wj4.y, wj4.z};
+    cs_pair<DIM>(b, mi, mj, pi.w, pj.w, Mi, b.cpos[cj].w, vi, vj, wi, wj, d, F, eF, T, eT);
+  };
+  if (use_list) {
+    const int n = b.ncnt[t];
+    const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
+    prefetch_list_block(b, t, n);
+    for (int k = 0; k < n; ++k) {
+      const uint32_t e = (uint32_t)nb[k * 32];
+      visit((int)(e & kEntrySlot), (e & kEntryImage) != 0u);
+    }
+  } else {
+    for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) {
+      if (j != (int)t) visit(j, true);
+    });
+  }
+  const float f[3] = {F[0] + eF[0], F[1] + eF[1], DIM == 3 ? F[2] + eF[2] : 0.0f};
+  float r[3] = {0.0f, 0.0f, 0.0f};
+  lever<DIM>(b, b.cq[ci], oi, r);
+  float tq[3] = {0.0f, 0.0f, 0.0f};
+  for (int a = 0; a < AD; ++a) tq[a] = T[a] + eT[a];
+  if (DIM == 3) {
+    tq[0] = tq[0] + (r[1] * f[2] - r[2] * f[1]);
+    tq[1] = tq[1] + (r[2] * f[0] - r[0] * f[2]);
+    tq[2] = tq[2] + (r[0] * f[1] - r[1] * f[0]);
+  } else {
+    tq[0] = tq[0] + (r[0] * f[1] - r[1] * f[0]);
+  }
+  b.sf[oi] = make_float4(f[0], f[1], f[2], 0.0f);
+  b.stq[oi] = make_float4(tq[0], tq[1], tq[2], 0.0f);
 }
 
 // Linear and rotational state of clump c as registers.
@@ -443,7 +518,7 @@ __global__ void k_rb_init(Bufs b, const float* __restrict__ pos, const float* __
   b.cbrad[c] = br;
 }
 
-// Upload: caller-order positions become the members' world positions.
+// Caller-order world positions of the members (upload, neighbour-list API).
 template <int DIM>
 __global__ void k_rb_world(Bufs b, float* __restrict__ pos) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -521,10 +596,12 @@ void launch_rb(int dim, const Bufs& b, int mode, cudaStream_t st) {
   if (b.P == 0) return;
   const unsigned int g = nblk_rb(b.P, 128), gc = nblk_rb(b.NC, 128);
   if (dim == 3) {
-    if (b.law == LAW_HERTZ) k_rb_force<3, LAW_HERTZ><<<g, 128, 0, st>>>(b);
+    if (b.law == LAW_CS) k_rb_cs_force<3><<<g, 128, 0, st>>>(b);
+    else if (b.law == LAW_HERTZ) k_rb_force<3, LAW_HERTZ><<<g, 128, 0, st>>>(b);
     else k_rb_force<3, LAW_SPRING><<<g, 128, 0, st>>>(b);
   } else {
-    if (b.law == LAW_HERTZ) k_rb_force<2, LAW_HERTZ><<<g, 128, 0, st>>>(b);
+    if (b.law == LAW_CS) k_rb_cs_force<2><<<g, 128, 0, st>>>(b);
+    else if (b.law == LAW_HERTZ) k_rb_force<2, LAW_HERTZ><<<g, 128, 0, st>>>(b);
     else k_rb_force<2, LAW_SPRING><<<g, 128, 0, st>>>(b);
   }
   if ((mode & 7) == MODE_FORCE_ONLY) return;
@@ -570,6 +647,12 @@ void launch_rb_unpack(int dim, const Bufs& b, float* pos, float* vel, float* frc
   const unsigned int g = nblk_rb(b.P, 256);
   if (dim == 3) k_rb_unpack<3><<<g, 256, 0, st>>>(b, pos, vel, frc, q, angv, torque, per_sphere ? 1 : 0);
   else k_rb_unpack<2><<<g, 256, 0, st>>>(b, pos, vel, frc, q, angv, torque, per_sphere ? 1 : 0);
+}
+
+void launch_rb_world(int dim, const Bufs& b, float* pos, cudaStream_t st) {
+  if (b.P == 0 || b.NC == 0) return;
+  if (dim == 3) k_rb_world<3><<<nblk_rb(b.P, 256), 256, 0, st>>>(b, pos);
+  else k_rb_world<2><<<nblk_rb(b.P, 256), 256, 0, st>>>(b, pos);
 }
 
 void launch_rb_energy(int dim, const Bufs& b, double* out, cudaStream_t st) {
@@ -646,7 +729,6 @@ int JdemHandle::setup_clumps(const JdemHostState* s, bool device_ptrs) {
   }
   const long long NC = (long long)count.size();
   if (NC == (long long)N && !offset) return JDEM_OK;  // spheres
-  if (b.law == LAW_CS) return fail(JDEM_ERR_UNSUPPORTED, "rigid clumps with Cundall-Strack contacts are not supported");
   std::vector<int32_t> start((size_t)NC + 1, 0), member(N);
   for (long long c = 0; c < NC; ++c) start[(size_t)c + 1] = start[(size_t)c] + count[(size_t)c];
   {

@@ -8,9 +8,9 @@ captured CUDA graphs; each call uploads the caller's state, runs, and reads
 the result back (the functional contract of the reference API).
 
 Configurations outside the GB300 hot path raise ``NotImplementedError``:
-rigid clumps with Cundall-Strack contacts, facets, bonded force models,
-force models other than ``spring``, ``hertz`` and ``cundallstrack``, user force functions, pending external
-forces and user pre/post-step actions.
+facets, bonded force models, force models other than ``spring``, ``hertz``
+and ``cundallstrack``, user force functions, pending external forces and
+user pre/post-step actions.
 """
 
 from __future__ import annotations
@@ -60,9 +60,6 @@ def _check_supported(state: State, system) -> None:
 
     if system.user_pre_step_actions is not _save_state_system or system.user_post_step_actions is not _save_state_system:
         raise NotImplementedError("user pre/post step actions are outside the GB300 hot path")
-    if _has_clumps(state):
-        if system.force_model.type_name == "cundallstrack":
-            raise NotImplementedError("rigid clumps with Cundall-Strack contacts are not supported by the GB300 engine")
     if state.facet_id.size and np.any(state.facet_id != -1):
         raise NotImplementedError("facets are outside the GB300 hot path")
 

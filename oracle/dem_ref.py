@@ -420,8 +420,9 @@ def _cross_w(w, r):
 def cs_pair(i, j, st, sy: OSystem):
     """``CundallStrackForce.force`` (``forces/cundall_strack.py:100-196``), vectorised over
     pairs: the force on ``i`` due to ``j`` and the torque on ``i``, concatenated
-    ``(..., dim + ang_dim)``."""
-    pos = st.pos_c
+    ``(..., dim + ang_dim)``.  Positions are ``state.pos`` (members' world positions for
+    clumps); velocities, spins and masses are the members' stored (clump) values."""
+    pos = world_pos(st)
     dt = pos.dtype.type
     d = pos.shape[-1]
     mi, mj = st.mat_id[i], st.mat_id[j]
@@ -575,10 +576,14 @@ def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     pos = world_pos(st)
     d = st.dim
     if sy.force_law == "cundallstrack":
-        # force and torque summed together; torque + cross(pos_p = 0, F) (cell_list.py:452-464)
+        # force and torque summed together; torque + cross(R(q) pos_p, F) (cell_list.py:452-464)
         ad = st.torque.shape[-1]
         ft = _traverse(st, sy, lambda i, j: cs_pair(i, j, st, sy), (d + ad,), pos.dtype, sum_dtype)
-        return ft[:, :d].astype(pos.dtype), ft[:, d:].astype(pos.dtype)
+        f, tq = ft[:, :d].astype(pos.dtype), ft[:, d:].astype(pos.dtype)
+        if st.rigid:
+            r = pos_p_rot(st)
+            tq = tq + (cross3(r, f) if d == 3 else r[:, 0:1] * f[:, 1:2] - r[:, 1:2] * f[:, 0:1])
+        return f, tq.astype(pos.dtype)
 
     def pair(i, j):
         return pair_force(i, j, pos, st.rad, st.mat_id, sy)
@@ -1118,10 +1123,11 @@ def create_neighbor_list(st: OState, sy: OSystem, cutoff, max_neighbors):
     scan (``_make_stencil_body`` ``:99-174``) with ``d_sq <= cutoff^2`` on the
     true-division displacement (``periodic.py:37-71``), prefix-sum packing
     (``_partition.py:102-150``), indices mapped back through ``perm``.
-    Returns ``(nl (N, max_neighbors) int, overflow bool)``.
+    Positions are ``state.pos`` (members' world positions for clumps; members of one
+    clump never list each other).  Returns ``(nl (N, max_neighbors) int, overflow bool)``.
     """
     N = st.N
-    pos = st.pos_c
+    pos = world_pos(st)
     t = pos.dtype.type
     cutoff_sq = t(cutoff) * t(cutoff)
     if max_neighbors == 0:

@@ -67,9 +67,16 @@ CASES = {
                       young=[1.0e3, 2.0e3], poisson=[0.3, 0.2], e=[0.5, 0.9], mu=[0.5, 0.2], mu_r=[0.0, 0.2]),
     # rigid clumps of one to three spheres (State.create with pos_p, q, clump_id, mass, inertia)
     "clump3d": dict(seed=1013, dim=3, N=40, domain="periodic", radii="clump", phi=0.35, vsig=0.3, dt=1e-3, wsig=1.0,
-                    strides=[1, 9, 20]),
+                    strides=[1, 9, 20], nl=3.0),
     "clump2d_refl": dict(seed=1014, dim=2, N=40, domain="reflect", radii="clump", phi=0.3, vsig=0.5, dt=1e-3,
-                         wsig=1.0, gravity=[0.0, -2.0], strides=[1, 9, 30]),
+                         wsig=1.0, gravity=[0.0, -2.0], strides=[1, 9, 30], nl=2.5),
+    # rigid clumps with Cundall-Strack contacts (sphere-centred contact arms, clump velocities)
+    "clump_cs3d": dict(seed=1015, dim=3, N=40, domain="periodic", radii="clump", phi=0.35, vsig=0.3, dt=5e-4,
+                       wsig=1.0, law="cundallstrack", strides=[1, 9, 20], young=[1.0e3, 3.0e3], poisson=[0.25, 0.3],
+                       e=[0.6, 0.8], mu=[0.4, 0.3], mu_r=[0.05, 0.1]),
+    "clump_cs2d_refl": dict(seed=1016, dim=2, N=40, domain="reflect", radii="clump", phi=0.3, vsig=0.5, dt=5e-4,
+                            wsig=1.0, gravity=[0.0, -2.0], law="cundallstrack", strides=[1, 9, 30],
+                            young=[1.0e3, 2.0e3], poisson=[0.3, 0.2], e=[0.5, 0.9], mu=[0.5, 0.2], mu_r=[0.0, 0.2]),
 }
 X64_CASES = ["per3d_bi", "refl2d_grav"]
 
@@ -135,9 +142,11 @@ def _clump_inputs(rng, c):
     wc = rng.normal(0.0, c["wsig"], (nc, ad))
     Mc = np.bincount(cid, weights=vol)
     Ic = np.stack([Mc * (0.2 + 0.05 * a) for a in range(ad)], 1)
+    nmat = len(c.get("young", [1.0e3]))
+    mat = rng.integers(0, nmat, size=N) if nmat > 1 else np.zeros(N, np.int64)
     f = np.float32
     return dict(pos=centres[cid].astype(f), vel=vc[cid].astype(f), rad=rad, ang_vel=wc[cid].astype(f),
-                mat_id=np.zeros(N, np.int32), box=np.full(dim, L, f), anchor=np.zeros(dim, f),
+                mat_id=mat.astype(np.int32), box=np.full(dim, L, f), anchor=np.zeros(dim, f),
                 pos_p=pos_p.astype(f), q=qc[cid].astype(f), clump_id=cid.astype(np.int32), mass_in=Mc[cid].astype(f),
                 inertia_in=Ic[cid].astype(f))
 

@@ -5,10 +5,11 @@ Each clump's state is held once on the device and its members' world positions
 pos_c + R(q) pos_p feed the cell list; contact forces and their lever-arm
 torques are summed per clump (ForceManager.apply, force_manager.py:338-425) and
 the integrators advance the clump.  The oracle is pinned by closed forms in
-test_oracle_pins.py (no reference test covers clump dynamics).  Bars: per-sphere
-force and torque <= 1e-5 floored relative error from identical inputs; 50-step
-rollouts <= 1e-4 in position; energies; bit-exact contact sets without
-same-clump pairs.
+test_oracle_pins.py and by the reference's own outputs for clumps (spring and
+Cundall-Strack contacts, periodic and reflect boxes, create_neighbor_list) in
+tests/golden.  Bars: per-sphere force and torque <= 1e-5 floored relative error
+from identical inputs; rollouts <= 1e-4 in position; energies; bit-exact
+contact sets and neighbour lists without same-clump pairs.
 """
 
 from __future__ import annotations
@@ -77,9 +78,9 @@ def engine(c, domain="periodic", linear="verlet", rotation="verletspiral", skin=
     return Engine(d, [desc], K, skin=skin)
 
 
-def upload(eng, c):
+def upload(eng, c, **extra):
     eng.upload(pos=c["pos_c"], rad=c["rad"], mass=c["mass"], vel=c["vel"], q=c["q"], ang_vel=c["ang_vel"],
-               inertia=c["inertia"], pos_p=c["pos_p"], clump_id=c["clump_id"])
+               inertia=c["inertia"], pos_p=c["pos_p"], clump_id=c["clump_id"], **extra)
 
 
 def ostate_sys(c, domain="periodic", linear="verlet", rotation="verletspiral", gravity=None):
@@ -182,18 +183,91 @@ def test_clump_reflect_rollout_matches_oracle(dim, steps=200):
     assert np.any(st.vel[:, 1] > 0.5)
 
 
-def test_clumps_with_cundall_strack_are_refused():
-    c = clump_system(n_clumps=50, seed=80)
-    beta, props = R.cs_tables([1e3], [0.3], [0.5], [0.3], [0.0])
-    desc = dict(n=c["N"], domain="periodic", linear="verlet", rotation="verletspiral", dt=1e-3,
-                box_size=np.full(3, c["L"], F32), anchor=np.zeros(3, F32), restitution=1.0,
-                gravity=np.zeros(3, F32), cell_size=1.0, search_range=1)
-    eng = Engine(3, [desc], beta, skin=0.1, force_law="cundallstrack", material_props=props)
+CS_MATS = dict(young=[1e3, 3e3], poisson=[0.25, 0.3], e=[0.6, 0.8], mu=[0.4, 0.3], mu_r=[0.05, 0.1])
+
+
+def cs_engine_sys(c, domain="periodic", gravity=None, rotation="verletspiral"):
+    """Clumps with Cundall-Strack contacts: two materials drawn per sphere."""
+    d = c["dim"]
+    beta, props = R.cs_tables(**CS_MATS)
+    c = dict(c, mat_id=np.random.default_rng(c["N"]).integers(0, 2, c["N"]).astype(np.int32))
+    g = np.zeros(d, F32) if gravity is None else np.asarray(gravity, F32)
+    desc = dict(n=c["N"], domain=domain, linear="verlet", rotation=rotation, dt=5e-4, box_size=np.full(d, c["L"], F32),
+                anchor=np.zeros(d, F32), restitution=1.0, gravity=g, cell_size=1.0, search_range=1)
+    eng = Engine(d, [desc], beta, skin=0.1, force_law="cundallstrack", material_props=props)
+    st, sy = ostate_sys(c, domain=domain, rotation=rotation, gravity=g)
+    st.mat_id = c["mat_id"]
+    sy.young_eff, sy.mat_props, sy.force_law, sy.dt = beta, props, "cundallstrack", F32(5e-4)
+    return c, eng, st, sy
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_clumps_with_cundall_strack_match_oracle(dim, steps=40):
+    """Cundall-Strack contacts between clumps (cundall_strack.py:100-196 on the members'
+    world positions with their clump's velocity, spin and mass; the lever torque
+    cross(R(q) pos_p, F) added, cell_list.py:452-464; clump sums, force_manager.py:338-425)."""
+    c = clump_system(n_clumps=400, dim=dim, seed=110 + dim, spin=2.0)
+    c, eng, st, sy = cs_engine_sys(c)
+    f64, t64 = R.cell_list_force(st, sy, sum_dtype=np.float64)
+    e_ref = R.compute_energy(st, sy)
+    st2, _ = R.step(st.copy(), sy, steps, sum_dtype=np.float64)
     try:
-        with pytest.raises(JdemError):
-            upload(eng, c)
+        upload(eng, c, mat_id=c["mat_id"])
+        eng.compute_force()
+        f0 = eng.download()
+        e = eng.energy()
+        upload(eng, c, mat_id=c["mat_id"])
+        eng.step(steps)
+        out = eng.download()
     finally:
         eng.close()
+    assert np.abs(t64).max() > 0
+    assert force_err(f0["force"], f64) <= 1e-5
+    assert force_err(f0["torque"], t64) <= 1e-5
+    for k in range(4):
+        assert abs(e[k] - e_ref[k]) <= 1e-5 * max(abs(e_ref[k]), 1e-3 * abs(e_ref[2]))
+    assert min_image_diff(out["pos_c"], st2.pos_c, np.full(dim, c["L"])) <= 1e-4
+    assert np.abs(out["vel"] - st2.vel).max() <= 1e-3 * max(1.0, np.abs(st2.vel).max())
+    assert np.abs(out["ang_vel"] - st2.ang_vel).max() <= 1e-3 * max(1.0, np.abs(st2.ang_vel).max())
+    assert np.abs(out["q"] - st2.q).max() <= 1e-4
+
+
+def test_clumps_with_cundall_strack_in_a_reflect_box(steps=100):
+    """2D clumps under gravity with the spiral integrator, wall impulses and friction."""
+    c = clump_system(n_clumps=300, dim=2, seed=121, phi=0.25, spin=2.0)
+    c["pos_c"] = (1.0 + c["pos_c"] * (c["L"] - 2.0) / c["L"]).astype(F32)
+    c, eng, st, sy = cs_engine_sys(c, domain="reflect", gravity=[0.0, -10.0], rotation="spiral")
+    st2, _ = R.step(st.copy(), sy, steps, sum_dtype=np.float64)
+    try:
+        upload(eng, c, mat_id=c["mat_id"])
+        eng.step(steps)
+        out = eng.download()
+    finally:
+        eng.close()
+    assert min_image_diff(out["pos_c"], st2.pos_c) <= 1e-4
+    assert np.abs(out["vel"] - st2.vel).max() <= 1e-3 * max(1.0, np.abs(st2.vel).max())
+    assert np.abs(out["ang_vel"] - st2.ang_vel).max() <= 1e-3 * max(1.0, np.abs(st2.ang_vel).max())
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_clump_neighbor_list_matches_oracle(dim):
+    """create_neighbor_list on a clump handle (cell_list.py:498-595): the members' world
+    positions, no member listing another member of its clump, bit for bit."""
+    c = clump_system(n_clumps=500, dim=dim, seed=130 + dim)
+    st, sy = ostate_sys(c)
+    cutoff = 2.5 * float(c["rad"].max())
+    want, want_ovf = R.create_neighbor_list(st, sy, cutoff, 40)
+    eng = engine(c)
+    try:
+        upload(eng, c)
+        nl, ovf = eng.neighbor_list(cutoff, 40)
+    finally:
+        eng.close()
+    assert bool(ovf) == bool(want_ovf)
+    assert np.array_equal(nl, want)
+    rows = np.repeat(np.arange(c["N"]), 40).reshape(c["N"], 40)
+    ok = nl >= 0
+    assert ok.sum() > 0 and not np.any(c["clump_id"][rows[ok]] == c["clump_id"][nl[ok]])
 
 
 def test_clumps_through_the_public_api():

@@ -93,13 +93,6 @@ def test_system_create_components_and_validation():
 def test_unsupported_configurations_raise_before_device_work():
     from jaxdem_gb300 import session
 
-    # rigid clumps are on the device path except with Cundall-Strack contacts
-    mats = [jdem.Material.create("elasticfrict", young=1e3, poisson=0.3, e=0.5, mu=0.3)]
-    table = jdem.MaterialTable.from_materials(mats)
-    st = jdem.State.create(pos=np.zeros((4, 3)), clump_id=[0, 0, 1, 1], mat_table=table)
-    sy = jdem.System.create(state=st, collider_type="CellList", mat_table=table, force_model_type="cundallstrack")
-    with pytest.raises(NotImplementedError):
-        session.engine_for(st, sy)
     st2 = jdem.State.create(pos=np.zeros((4, 3)))
     fm = jdem.ForceManager.create((4, 3), force_functions=[lambda p, s, y: (p, p)])
     sy2 = jdem.System.create(state=st2, collider_type="CellList", force_manager=fm)
