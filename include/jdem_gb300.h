@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 9
+#define JDEM_ABI_VERSION 10
 
 enum {
   JDEM_OK = 0,
@@ -327,9 +327,10 @@ typedef struct {
   double hbm_budget_bytes;   /* admission limit on the resident footprint (<= 0: 150e9) */
   float skin;                /* binning skin of the batch */
   float young;               /* spring stiffness when n_materials is 0 */
-  int32_t force_law;         /* JDEM_FORCE_SPRING or JDEM_FORCE_HERTZ (System.force_model) */
+  int32_t force_law;         /* JDEM_FORCE_SPRING, _HERTZ or _CUNDALL_STRACK (System.force_model) */
   int32_t n_materials;       /* size M of young_eff (0: one material of stiffness `young`) */
   const float* young_eff;    /* M*M pair constants, as JdemConfig.young_eff (copied at create) */
+  const float* material_props; /* Cundall-Strack only: M*4, as JdemConfig.material_props (copied) */
 } JdemServeConfig;
 
 typedef struct {

@@ -692,7 +692,8 @@ int JdemHandle::upload(const JdemHostState* s, bool device_ptrs) {
 // system's rotation integrator has a non-trivial state to advance.
 int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
                                 const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s,
-                                const int32_t* d_mat, const float* d_q, const float* d_w, bool rot) {
+                                const int32_t* d_mat, const float* d_q, const float* d_w, bool rot,
+                                const float* d_torque) {
   JDEM_CUDA_TRY(this, cudaSetDevice(dev));
   int rc = plan_grid(rmax_s, lo_s, hi_s);
   if (rc) return rc;
@@ -711,7 +712,10 @@ int JdemHandle::upload_resident(const float* d_pos, const float* d_vel, const fl
     JDEM_CUDA_TRY(this, cudaMemsetAsync(st_fixed, 0, N, stream));
     if (d_w) JDEM_CUDA_TRY(this, cudaMemcpyAsync(this->d_w, d_w, N * ad * 4, k, stream));
     else JDEM_CUDA_TRY(this, cudaMemsetAsync(this->d_w, 0, N * ad * 4, stream));
-    JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
+    // the torque of the last step: the next call's first rotational half-kick under
+    // Cundall-Strack contacts (k_cs_rot_pre) reads it
+    if (d_torque) JDEM_CUDA_TRY(this, cudaMemcpyAsync(d_tq, d_torque, N * ad * 4, k, stream));
+    else JDEM_CUDA_TRY(this, cudaMemsetAsync(d_tq, 0, N * ad * 4, stream));
     launch_default_inertia(dim, (long long)N, st_mass, st_rad, d_inertia, stream);
     if (d_q) JDEM_CUDA_TRY(this, cudaMemcpyAsync(this->d_q, d_q, N * 16, k, stream));
     else launch_identity_q((float4*)this->d_q, (long long)N, stream);

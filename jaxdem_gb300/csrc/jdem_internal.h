@@ -135,7 +135,7 @@ struct JdemHandle {
   int upload_resident(const float* d_pos, const float* d_vel, const float* d_frc, const float* d_rad,
                       const float* d_mass, const float* rmax_s, const float* lo_s, const float* hi_s,
                       const int32_t* d_mat = nullptr, const float* d_q = nullptr, const float* d_w = nullptr,
-                      bool rot = false);
+                      bool rot = false, const float* d_torque = nullptr);
   int plan_tiles();
   int plan_list(int cap);
   int reset_ctl();

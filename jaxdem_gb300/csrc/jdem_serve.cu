@@ -64,13 +64,16 @@ struct Staging {
   float *pos = nullptr, *vel = nullptr, *frc = nullptr, *rad = nullptr, *mass = nullptr;
   float *mat = nullptr;  // int32 material ids, moved as 4-byte words
   float *q = nullptr, *w = nullptr;
+  float* tq = nullptr;  // torque of the last step (Cundall-Strack: the next half-kick reads it)
   long long cap = 0;
 };
 
 void free_staging(Staging& s) {
-  for (float* p : {s.pos, s.vel, s.frc, s.rad, s.mass, s.mat, s.q, s.w}) cudaFree(p);
+  for (float* p : {s.pos, s.vel, s.frc, s.rad, s.mass, s.mat, s.q, s.w, s.tq}) cudaFree(p);
   s = Staging{};
 }
+
+constexpr int kStagedArrays = 9;
 
 }  // namespace
 
@@ -103,6 +106,7 @@ struct JdemServer {
   int64_t n_active = 0;    // admitted and not yet finished (guarded by mtx)
   JdemServeStats stats{};
   std::vector<float> young_eff;  // M * M pair constants of the force law
+  std::vector<float> mat_props;  // Cundall-Strack: M * 4 per-material properties
   std::string err;
 
   int fail(int code, const std::string& m) {
@@ -132,7 +136,8 @@ int JdemServer::ensure_staging(Staging& s, long long n) {
   int d = cfg.dim, ad = d == 3 ? 3 : 1;
   if (dmalloc((void**)&s.pos, 4 * cap * d) || dmalloc((void**)&s.vel, 4 * cap * d) ||
       dmalloc((void**)&s.frc, 4 * cap * d) || dmalloc((void**)&s.rad, 4 * cap) || dmalloc((void**)&s.mass, 4 * cap) ||
-      dmalloc((void**)&s.mat, 4 * cap) || dmalloc((void**)&s.q, 16 * cap) || dmalloc((void**)&s.w, 4 * cap * ad))
+      dmalloc((void**)&s.mat, 4 * cap) || dmalloc((void**)&s.q, 16 * cap) || dmalloc((void**)&s.w, 4 * cap * ad) ||
+      dmalloc((void**)&s.tq, 4 * cap * ad))
     return fail(JDEM_ERR_OOM, "serve: staging allocation failed");
   s.cap = cap;
   return JDEM_OK;
@@ -166,6 +171,7 @@ int JdemServer::repack(std::vector<Req*>& next) {
     out.force = st[cur].frc;
     out.q = st[cur].q;
     out.ang_vel = st[cur].w;
+    out.torque = st[cur].tq;
     rc = h->download(&out, true);
     if (rc) return fail(rc, std::string("serve: download ") + h->err);
     cur_valid = true;
@@ -194,6 +200,7 @@ int JdemServer::repack(std::vector<Req*>& next) {
         cudaMemcpyAsync(st[nxt].mat + o, r->h_mat, 4 * n, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(st[nxt].q + o * 4, r->h_q, 16 * n, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(st[nxt].w + o * ad, r->h_w, 4 * n * ad, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(st[nxt].tq + o * ad, 0, 4 * n * ad, s);
       }
     }
     descs.push_back(r->desc);
@@ -208,23 +215,23 @@ int JdemServer::repack(std::vector<Req*>& next) {
   if (nseg > 0) {
     // segment table and array pointers, copied with the stream (then synchronised)
     if (!d_seg) {
-      if (dmalloc((void**)&d_src, sizeof(float*) * 8) || dmalloc((void**)&d_dst, sizeof(float*) * 8) ||
-          dmalloc((void**)&d_width, sizeof(int) * 8))
+      if (dmalloc((void**)&d_src, sizeof(float*) * kStagedArrays) ||
+          dmalloc((void**)&d_dst, sizeof(float*) * kStagedArrays) || dmalloc((void**)&d_width, sizeof(int) * kStagedArrays))
         return fail(JDEM_ERR_OOM, "serve: table allocation failed");
     }
     cudaFree(d_seg);
     d_seg = nullptr;
     if (dmalloc((void**)&d_seg, sizeof(long long) * seg.size())) return fail(JDEM_ERR_OOM, "serve: segment table");
-    const float* src[8] = {st[cur].pos, st[cur].vel, st[cur].frc, st[cur].rad, st[cur].mass,
-                           st[cur].mat,  st[cur].q,   st[cur].w};
-    float* dst[8] = {st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass,
-                     st[nxt].mat, st[nxt].q,   st[nxt].w};
-    int width[8] = {d, d, d, 1, 1, 1, 4, ad};
+    const float* src[kStagedArrays] = {st[cur].pos, st[cur].vel, st[cur].frc, st[cur].rad, st[cur].mass,
+                                       st[cur].mat,  st[cur].q,   st[cur].w,   st[cur].tq};
+    float* dst[kStagedArrays] = {st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass,
+                                 st[nxt].mat, st[nxt].q,   st[nxt].w,   st[nxt].tq};
+    int width[kStagedArrays] = {d, d, d, 1, 1, 1, 4, ad, ad};
     cudaMemcpyAsync(d_seg, seg.data(), sizeof(long long) * seg.size(), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_src, src, sizeof(src), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_dst, dst, sizeof(dst), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_width, width, sizeof(width), cudaMemcpyHostToDevice, s);
-    launch_segcopy(d_seg, nseg, 8, d_src, d_dst, d_width, s);
+    launch_segcopy(d_seg, nseg, kStagedArrays, d_src, d_dst, d_width, s);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(JDEM_ERR_CUDA, "serve: repack copies failed");
   if (next.empty()) {
@@ -236,7 +243,7 @@ int JdemServer::repack(std::vector<Req*>& next) {
   rc = h->rebind(descs.data(), (int)descs.size());
   if (rc) return fail(rc, std::string("serve: rebind ") + h->err);
   rc = h->upload_resident(st[nxt].pos, st[nxt].vel, st[nxt].frc, st[nxt].rad, st[nxt].mass, rmax.data(), lo.data(),
-                          hi.data(), (const int32_t*)st[nxt].mat, st[nxt].q, st[nxt].w, rot);
+                          hi.data(), (const int32_t*)st[nxt].mat, st[nxt].q, st[nxt].w, rot, st[nxt].tq);
   if (rc) return fail(rc, std::string("serve: upload ") + h->err);
   active = next;
   cur = nxt;
@@ -255,6 +262,7 @@ int JdemServer::finish(std::vector<Req*>& done) {
   out.force = st[cur].frc;
   out.q = st[cur].q;
   out.ang_vel = st[cur].w;
+  out.torque = st[cur].tq;
   int rc = h->download(&out, true);
   if (rc) return fail(rc, std::string("serve: download ") + h->err);
   cur_valid = true;
@@ -459,25 +467,29 @@ int jdem_serve_create(const JdemServeConfig* cfg, JdemServer** out) {
   d.linear_integrator = JDEM_LIN_VERLET;
   d.dt = 1e-3f;
   for (int a = 0; a < 3; ++a) d.box_size[a] = 1.0f;
-  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ) {
+  const bool cs = cfg->force_law == JDEM_FORCE_CUNDALL_STRACK;
+  if (cfg->force_law != JDEM_FORCE_SPRING && cfg->force_law != JDEM_FORCE_HERTZ && !cs) {
     delete s;
-    return JDEM_ERR_UNSUPPORTED;  // Cundall-Strack needs per-material tables the server does not take
+    return JDEM_ERR_UNSUPPORTED;
   }
-  if (cfg->n_materials < 0 || (cfg->n_materials > 0 && !cfg->young_eff)) {
+  if (cfg->n_materials < 0 || (cfg->n_materials > 0 && !cfg->young_eff) ||
+      (cs && (cfg->n_materials <= 0 || !cfg->material_props))) {
     delete s;
-    return JDEM_ERR_BAD_ARG;
+    return JDEM_ERR_BAD_ARG;  // Cundall-Strack takes its beta and per-material tables explicitly
   }
   float young = cfg->young > 0 ? cfg->young : 1e3f;
   const int M = cfg->n_materials > 0 ? cfg->n_materials : 1;
   try {
     if (cfg->n_materials > 0) s->young_eff.assign(cfg->young_eff, cfg->young_eff + (size_t)M * M);
     else s->young_eff.assign(1, young);
+    if (cs) s->mat_props.assign(cfg->material_props, cfg->material_props + (size_t)M * 4);
   } catch (...) {
     delete s;
     return JDEM_ERR_OOM;
   }
   s->cfg.n_materials = M;
-  s->cfg.young_eff = nullptr;  // the server keeps its own copy
+  s->cfg.young_eff = nullptr;  // the server keeps its own copies
+  s->cfg.material_props = nullptr;
   JdemConfig ec{};
   ec.dim = cfg->dim;
   ec.n_systems = 1;
@@ -486,6 +498,7 @@ int jdem_serve_create(const JdemServeConfig* cfg, JdemServer** out) {
   ec.n_materials = M;
   ec.young_eff = s->young_eff.data();
   ec.force_law = cfg->force_law;
+  ec.material_props = cs ? s->mat_props.data() : nullptr;
   ec.chunk_steps = s->cfg.chunk_steps;
   ec.device = cfg->device;
   ec.graph_mode = 2;  // the batch changes between epochs: direct launches
@@ -607,8 +620,8 @@ int jdem_serve_submit(JdemServer* s, const JdemRequest* req, int64_t* id) {
   if (req->ang_vel) std::memcpy(r->h_w, req->ang_vel, 4 * n * ad);
   else std::memset(r->h_w, 0, 4 * n * ad);
   // resident footprint: slot arrays (both copies), staging (both layouts, with the
-  // material id and rotational state), both Verlet lists
-  r->bytes = n * (size_t)(2 * 96 + 2 * 4 * (3 * d + 3 + 4 + ad) + 8 * 64);
+  // material id, rotational state and torque), both Verlet lists
+  r->bytes = n * (size_t)(2 * 96 + 2 * 4 * (3 * d + 3 + 4 + 2 * ad) + 8 * 64);
   if ((double)r->bytes > s->cfg.hbm_budget_bytes) {
     // could never be admitted: reject instead of blocking the queue
     free_req(r);

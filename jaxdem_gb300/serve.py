@@ -4,8 +4,8 @@ into a continuously batched device handle (``jdem_serve_*`` in
 
 A request is ``System.step(state, system, n=steps)`` on one independent
 sphere system: its own domain, integrators (rotation included), dt, material
-ids and rotational state, under the server's force law (spring or Hertz) and
-material table.  ``Server`` wraps one dimension; ``run_stream`` replays a
+ids and rotational state, under the server's force law (spring, Hertz or
+Cundall-Strack) and material table.  ``Server`` wraps one dimension; ``run_stream`` replays a
 timed arrival stream on a 2D and a 3D server at once and reports latency
 percentiles and throughput; ``run_one_at_a_time`` serves the same stream with
 the plain kernel, one request after another, for comparison.
@@ -32,7 +32,7 @@ class ServeConfig(C.Structure):
     _fields_ = [("dim", C.c_int32), ("device", C.c_int32), ("max_active", C.c_int32), ("chunk_steps", C.c_int32),
                 ("target_particles", C.c_int64), ("hbm_budget_bytes", C.c_double), ("skin", C.c_float),
                 ("young", C.c_float), ("force_law", C.c_int32), ("n_materials", C.c_int32),
-                ("young_eff", C.c_void_p)]
+                ("young_eff", C.c_void_p), ("material_props", C.c_void_p)]
 
 
 class RequestStruct(C.Structure):
@@ -101,19 +101,27 @@ class Server:
     def __init__(self, dim: int, *, max_active: int = 1024, chunk_steps: int = 50,
                  target_particles: int = 4 << 20, hbm_budget_gb: float = 150.0, skin: Optional[float] = None,
                  rmax: float = 0.6, young: float = K_SPRING, device: int = 0, force_law: str = "spring",
-                 young_eff: Optional[np.ndarray] = None):
+                 young_eff: Optional[np.ndarray] = None, material_props: Optional[np.ndarray] = None):
         """``young_eff`` (M, M): the force law's pair constant per material pair (spring k,
-        Hertz (4/3) E*); None: one material of stiffness ``young``."""
+        Hertz (4/3) E*, Cundall-Strack beta); None: one material of stiffness ``young``.
+        ``material_props`` (M, 4): Cundall-Strack's (young, shear modulus, mu, mu_r) per
+        material (both tables required for ``force_law="cundallstrack"``)."""
         self.lib = _lib()
         self.dim = dim
-        if force_law not in ("spring", "hertz"):
-            raise ValueError("the server runs the spring or Hertz law")
+        if force_law not in FORCE_LAW:
+            raise ValueError(f"unknown force law '{force_law}'")
+        if force_law == "cundallstrack" and (young_eff is None or material_props is None):
+            raise ValueError("Cundall-Strack needs young_eff (beta) and material_props")
         table = None if young_eff is None else np.ascontiguousarray(young_eff, F32)
+        props = None if material_props is None else np.ascontiguousarray(material_props, F32).reshape(-1, 4)
+        if props is not None and table is not None and props.shape[0] != table.shape[0]:
+            raise ValueError("material_props must have one row per material")
         cfg = ServeConfig(dim=dim, device=device, max_active=max_active, chunk_steps=chunk_steps,
                           target_particles=int(target_particles), hbm_budget_bytes=hbm_budget_gb * 1e9,
                           skin=float(default_skin(rmax) if skin is None else skin), young=float(young),
                           force_law=FORCE_LAW[force_law], n_materials=0 if table is None else table.shape[0],
-                          young_eff=None if table is None else table.ctypes.data)
+                          young_eff=None if table is None else table.ctypes.data,
+                          material_props=None if props is None or force_law != "cundallstrack" else props.ctypes.data)
         h = C.c_void_p()
         rc = self.lib.jdem_serve_create(C.byref(cfg), C.byref(h))
         if rc:

@@ -154,10 +154,10 @@ def test_release_while_batch_continues():
     assert min_image_diff(r["pos_c"], engine_result(long_)["pos_c"], long_.box_size) <= 1e-5
 
 
-def _engine_alone(w, law, young, mat=None, ang=None, rotation=""):
+def _engine_alone(w, law, young, mat=None, ang=None, rotation="", props=None):
     d = w.desc()
     d["rotation"] = rotation
-    eng = Engine(w.dim, [d], young, skin=default_skin(0.6), force_law=law)
+    eng = Engine(w.dim, [d], young, skin=default_skin(0.6), force_law=law, material_props=props)
     try:
         eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat, ang_vel=ang)
         eng.step(w.steps)
@@ -205,3 +205,42 @@ def test_hertz_materials_rotation_alone_equals_in_mix_and_engine(dim):
     assert not np.allclose(mix[1]["q"][:, 0], 1.0), "the spins should have rotated the spheres"
     assert min_image_diff(mix[2]["pos_c"], ref_b["pos_c"], b.box_size) <= 1e-5
     assert np.allclose(mix[2]["q"], np.array([1, 0, 0, 0], F32))
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_cundall_strack_alone_equals_in_mix_and_engine(dim):
+    """A Cundall-Strack server (two elasticfrict materials, rolling friction): a spinning
+    request gives the same state alone, in a mix whose repacks move it between epochs (its
+    last torque travels with it: the next half-kick reads it), and on a standalone engine
+    handle (positions 1e-5, q and spin 1e-5)."""
+    from oracle import dem_ref as R
+
+    beta, props = R.cs_tables(young=[1e3, 3e3], poisson=[0.25, 0.3], e=[0.6, 0.8], mu=[0.4, 0.3],
+                              mu_r=[0.05, 0.1])
+    rot = "verletspiral" if dim == 3 else "spiral"
+    ad = 3 if dim == 3 else 1
+    rng = np.random.default_rng(70 + dim)
+    a = req(1200, 41 + dim, dim=dim, phi=0.45, steps=130)
+    a_mat = rng.integers(0, 2, a.N).astype(np.int32)
+    a_ang = rng.normal(0, 2.0, (a.N, ad)).astype(F32)
+
+    def serve(items):
+        s = Server(dim, force_law="cundallstrack", young_eff=beta, material_props=props, chunk_steps=20)
+        try:
+            ids = [s.submit(w, mat_id=m, ang_vel=g, rotation=r) for w, m, g, r in items]
+            s.drain(120)
+            return [s.result(i) for i in ids]
+        finally:
+            s.close()
+
+    alone = serve([(a, a_mat, a_ang, rot)])[0]
+    mix = serve([(req(400, 51, dim=dim, steps=30), None, None, ""), (a, a_mat, a_ang, rot),
+                 (req(2000, 52, dim=dim, phi=0.35, steps=70), None, None, "")])
+    ref = _engine_alone(a, "cundallstrack", beta, a_mat, a_ang, rot, props=props)
+    for got in (alone, mix[1]):
+        assert got["info"]["state"] == "done"
+        assert min_image_diff(got["pos_c"], ref["pos_c"], a.box_size) <= 1e-5
+        assert np.allclose(got["vel"], ref["vel"], atol=1e-5 * max(1.0, np.abs(ref["vel"]).max()))
+        assert np.allclose(got["q"], ref["q"], atol=1e-5)
+        assert np.allclose(got["ang_vel"], ref["ang_vel"], atol=1e-5 * max(1.0, np.abs(ref["ang_vel"]).max()))
+    assert all(m["info"]["state"] == "done" for m in mix)
