@@ -105,6 +105,9 @@ class OSystem:
     inv_box_size: Optional[np.ndarray] = None
     force_law: str = "spring"  # "spring" | "hertz" | "cundallstrack" (forces/*.py)
     mat_props: Optional[np.ndarray] = None  # cundallstrack: (M, 4) young, shear modulus, mu, mu_r
+    # NeighborList collider (colliders/neighbor_list.py): cutoff, skin, max_neighbors and the
+    # cached list, reference positions and build count; None for the cell list
+    nlist: Optional[dict] = None
 
     def __post_init__(self) -> None:
         if self.inv_box_size is None:
@@ -600,6 +603,67 @@ def cell_list_force(st: OState, sy: OSystem, sum_dtype=None):
     return f, tq.astype(pos.dtype)
 
 
+def neighbor_list_collider(cutoff, skin, max_neighbors, dtype=np.float32):
+    """A NeighborList collider's cache before its first build (``neighbor_list.py:287-420``)."""
+    return {"cutoff": dtype(cutoff), "skin": dtype(skin), "max": int(max_neighbors), "nl": None, "old_pos": None,
+            "builds": 0}
+
+
+def neighbor_list_force(st: OState, sy: OSystem):
+    """``NeighborList.compute_force`` (``colliders/neighbor_list.py:594-661``).
+
+    ``_check_and_rebuild`` (``:58-130``): the list is rebuilt when the largest unwrapped
+    displacement since the last build exceeds skin / 2 (squared: skin**2 / 4) or before the
+    first build, by the cell list's ``create_neighbor_list`` at cutoff + skin (``_rebuild``,
+    ``:545-592``).  Each particle then sums its row in list order, padding and excluded
+    entries as zero terms (``jnp.sum`` over the row), and adds cross(R(q) pos_p, F) to the
+    torque sum.  Updates the cache in ``sy.nlist``; returns ``(force, torque)``.
+    """
+    c = sy.nlist
+    pos = world_pos(st)
+    dt = pos.dtype.type
+    rebuild = c["builds"] == 0
+    if not rebuild:
+        disp = pos - c["old_pos"]
+        rebuild = bool(np.max(sumsq(disp)) > c["skin"] ** 2 / dt(4))
+    if rebuild:
+        c["nl"], _ = create_neighbor_list(st, sy, dt(c["cutoff"] + c["skin"]), c["max"])
+        c["old_pos"] = pos.copy()
+        c["builds"] += 1
+    nl = c["nl"]
+    N, d = pos.shape
+    ad = st.torque.shape[-1]
+    f = np.zeros((N, d), pos.dtype)
+    tq = np.zeros((N, ad), pos.dtype)
+    iota = np.arange(N)
+    for m in range(nl.shape[1]):
+        j = nl[:, m]
+        safe = np.maximum(j, 0)
+        valid = (j != -1) & valid_mask(st.clump_id[iota], st.clump_id[safe], st.bond_id, safe,
+                                       sy.interact_same_bond_id)
+        if sy.force_law == "cundallstrack":
+            ft = cs_pair(iota, safe, st, sy)
+            fi, ti = ft[:, :d], ft[:, d:]
+        else:
+            fi, ti = pair_force(iota, safe, pos, st.rad, st.mat_id, sy), np.zeros((N, ad), pos.dtype)
+        fi = np.where(valid[:, None], fi, dt(0))
+        ti = np.where(valid[:, None], ti, dt(0))
+        # jnp.sum over the row: the first entry, then left to right
+        f = fi if m == 0 else f + fi
+        tq = ti if m == 0 else tq + ti
+    r = pos_p_rot(st)
+    tq = tq + (cross3(r, f) if d == 3 else r[:, 0:1] * f[:, 1:2] - r[:, 1:2] * f[:, 0:1])
+    return f.astype(pos.dtype), tq.astype(pos.dtype)
+
+
+def collider_force(st: OState, sy: OSystem, sum_dtype=None):
+    """``system.collider.compute_force``: the NeighborList collider when ``sy.nlist`` is set,
+    else the cell list."""
+    if sy.nlist is not None:
+        return neighbor_list_force(st, sy)
+    return cell_list_force(st, sy, sum_dtype)
+
+
 def cell_list_energy(st: OState, sy: OSystem, sum_dtype=None):
     """``DynamicCellList.compute_potential_energy`` (``cell_list.py:466-496``), pair term x0.5 (``_partition.py:39-51``)."""
     pos = world_pos(st)
@@ -1024,7 +1088,7 @@ def step_once(st: OState, sy: OSystem, sum_dtype=None, collider="celllist"):
         st.force = naive_force(st, sy)
         st.torque = np.zeros_like(st.torque)
     else:
-        st.force, st.torque = cell_list_force(st, sy, sum_dtype)
+        st.force, st.torque = collider_force(st, sy, sum_dtype)
     st = force_manager_apply(st, sy)
     if sy.linear == "verlet":
         st = vv_after(st, sy)

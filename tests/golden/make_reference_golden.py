@@ -74,6 +74,11 @@ CASES = {
     "clump_cs3d": dict(seed=1015, dim=3, N=40, domain="periodic", radii="clump", phi=0.35, vsig=0.3, dt=5e-4,
                        wsig=1.0, law="cundallstrack", strides=[1, 9, 20], young=[1.0e3, 3.0e3], poisson=[0.25, 0.3],
                        e=[0.6, 0.8], mu=[0.4, 0.3], mu_r=[0.05, 0.1]),
+    # the NeighborList collider (cached Verlet list with skin, rebuilt on displacement)
+    "nlist3d": dict(seed=1017, dim=3, N=96, domain="periodic", radii="bi", phi=0.5, vsig=0.3, dt=5e-4,
+                    collider="NeighborList", nl_skin=0.15, strides=[1, 9, 30]),
+    "nlist2d_refl": dict(seed=1018, dim=2, N=96, domain="reflect", radii="poly", phi=0.6, vsig=0.5, dt=5e-4,
+                         gravity=[0.0, -1.0], collider="NeighborList", nl_skin=0.1, strides=[1, 9, 30]),
     "clump_cs2d_refl": dict(seed=1016, dim=2, N=40, domain="reflect", radii="clump", phi=0.3, vsig=0.5, dt=5e-4,
                             wsig=1.0, gravity=[0.0, -2.0], law="cundallstrack", strides=[1, 9, 30],
                             young=[1.0e3, 2.0e3], poisson=[0.3, 0.2], e=[0.5, 0.9], mu=[0.5, 0.2], mu_r=[0.0, 0.2]),
@@ -182,16 +187,21 @@ def run_case(jd, name, c, x64):
     if c["domain"] == "reflect":
         domain_kw["restitution_coefficient"] = float(c.get("restitution", 1.0))
     fm_kw = {"gravity": c["gravity"]} if c.get("gravity") else None
+    coll = c.get("collider", "CellList")
+    coll_kw = {"state": state}
+    if coll == "NeighborList":
+        coll_kw.update(cutoff=2.0 * float(inp["rad"].max()), skin=float(c["nl_skin"]), max_neighbors=48)
     system = jd.System.create(
-        state.shape, dt=c["dt"], domain_type=c["domain"], domain_kw=domain_kw, collider_type="CellList",
-        collider_kw={"state": state}, mat_table=mat_table, force_model_type=c.get("law", "spring"),
+        state.shape, dt=c["dt"], domain_type=c["domain"], domain_kw=domain_kw, collider_type=coll,
+        collider_kw=coll_kw, mat_table=mat_table, force_model_type=c.get("law", "spring"),
         linear_integrator_type=c.get("linear", "verlet"), rotation_integrator_type=c.get("rotation", "verletspiral"),
         force_manager_kw=fm_kw)
     out = {k: np.asarray(v) for k, v in inp.items()}
     out["mass"] = np.asarray(state.mass)
     out["inertia"] = np.asarray(state.inertia)
     out["young_eff"] = np.asarray(system.mat_table.young_eff)
-    out["cell_size"] = np.asarray(system.collider.cell_size)
+    cl = system.collider.secondary_collider if coll == "NeighborList" else system.collider
+    out["cell_size"] = np.asarray(cl.cell_size)
     # compute_force from the inputs (cell_list.py:434-464) and the energies (thermal.py:127-177)
     s0, sy0 = system.collider.compute_force(state, system)
     out["force0"] = np.asarray(s0.force)
@@ -224,6 +234,11 @@ def run_case(jd, name, c, x64):
         snaps["ke"].append(np.asarray(jd.utils.thermal.compute_translational_kinetic_energy(st)))
     for k, v in snaps.items():
         out["snap_" + k] = np.stack(v)
+    if coll == "NeighborList":
+        out["nl_builds"] = np.asarray(sy.collider.n_build_times)
+        out["nl_max"] = np.asarray(system.collider.max_neighbors)
+        out["nl_list_cutoff"] = np.asarray(system.collider.cutoff)
+        out["nl_list_skin"] = np.asarray(system.collider.skin)
     out["snap_steps"] = np.cumsum(c["strides"]).astype(np.int32)
     out["meta"] = np.array(json.dumps({"case": name, "x64": x64, **c}))
     return out

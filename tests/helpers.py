@@ -92,7 +92,9 @@ def reference_osystem(d, dtype=np.float32):
                      dt=dtype(m["dt"]), cell_size=dtype(d["cell_size"]), neighbor_mask=mask, gravity=grav,
                      restitution=dtype(m.get("restitution", 1.0)), linear=m.get("linear", "verlet"),
                      rotation=m.get("rotation", "verletspiral"), force_law=law,
-                     mat_props=None if props is None else np.asarray(props, dtype))
+                     mat_props=None if props is None else np.asarray(props, dtype),
+                     nlist=None if m.get("collider", "CellList") != "NeighborList" else R.neighbor_list_collider(
+                         d["nl_list_cutoff"], d["nl_list_skin"], int(d["nl_max"]), dtype))
 
 
 def reference_cs_tables(d):

@@ -14,7 +14,9 @@ reflect with restitution 0.8 and gravity, 3D free domain, VV-spiral and spiral r
 with random spins, Hertz law, two materials, direct Euler, a periodic box of two cells
 per axis (the reference de-duplicates the stencil), Cundall-Strack with two "elasticfrict"
 materials and rolling friction (3D periodic; 2D reflect with gravity and the spiral
-integrator), and rigid clumps of one to three spheres (3D periodic; 2D reflect with gravity).
+integrator), rigid clumps of one to three spheres (3D periodic; 2D reflect with gravity), with
+and without Cundall-Strack contacts, and the NeighborList collider (cached list with skin,
+rebuilt on displacement; 3D periodic, 2D reflect with gravity).
 
 One reduction is not bit-reproducible by construction: the reference sums each particle's
 per-stencil-cell accumulators with ``x.sum(axis=0)`` (``colliders/cell_list.py:255-256``),
@@ -40,7 +42,7 @@ X64_CASES = ["per3d_bi", "refl2d_grav"]
 
 
 def test_fixture_set_is_complete():
-    assert len(CASES) >= 15, CASES
+    assert len(CASES) >= 19, CASES
     laws = {load_reference_case(c)["meta"].get("law", "spring") for c in CASES}
     assert laws == {"spring", "hertz", "cundallstrack"}
     assert sum("clump_id" in load_reference_case(c) for c in CASES) >= 2
@@ -59,8 +61,9 @@ def _same(a, b, loose, rtol=1e-6, atol=0.0):
 def test_numpy_oracle_reproduces_reference_bit_for_bit(name):
     d = load_reference_case(name)
     loose = _torque_order_free(d)
-    sy, st = reference_osystem(d), reference_ostate(d)
-    f0, t0 = R.cell_list_force(st, sy)
+    st = reference_ostate(d)
+    f0, t0 = R.collider_force(st, reference_osystem(d))
+    sy = reference_osystem(d)
     assert np.array_equal(f0, d["force0"]), f"{name}: compute_force differs (err {force_err(f0, d['force0'])})"
     assert _same(t0, d["torque0"], loose, atol=1e-6 * np.abs(d["torque0"]).max())
     e = R.compute_energy(st, sy)
@@ -94,9 +97,11 @@ def test_neighbor_list_reproduces_reference(name):
 
 
 def _c_covers(d):
-    """The C restatement covers smooth spheres under the spring and Hertz laws."""
+    """The C restatement covers smooth spheres under the spring and Hertz laws with the
+    cell-list collider."""
     return (not np.any(d["ang_vel"]) and "clump_id" not in d
-            and d["meta"].get("law", "spring") in ("spring", "hertz"))
+            and d["meta"].get("law", "spring") in ("spring", "hertz")
+            and d["meta"].get("collider", "CellList") == "CellList")
 
 
 C_CASES = [c for c in CASES if _c_covers(load_reference_case(c))]
