@@ -7,7 +7,9 @@ the C/OpenMP oracle (float64 force accumulation).
   * 4,194,304 polydisperse disks in a reflecting box with gravity: the same checks over
     10 steps;
   * 4096 monodisperse spheres for the configured 1000 steps: positions <= 1e-4 and the
-    total-energy trace (every 100 steps) against the oracle's.
+    total-energy trace (every 100 steps) against the oracle's;
+  * 96 systems of the batched configuration's size and density distribution in one
+    handle, each held against the oracle run on it alone.
 
 These runs take the code paths only large grids take (thousands of list-build bricks,
 87^3 and 1820^2 binning grids, list-capacity planning at full density), which the
@@ -135,3 +137,37 @@ def test_c1_as_configured_1000_steps():
     tot_g, tot_r = gpu_e.sum(1), ref_e.sum(1)
     assert np.allclose(tot_g, tot_r, rtol=1e-5, atol=1e-6), (tot_g, tot_r)
     assert np.allclose(gpu_e, ref_e, rtol=1e-4, atol=1e-5)
+
+
+def test_c4_style_uneven_batch_against_the_oracle(steps=100):
+    """Systems of the batched configuration's distribution (log-uniform sizes, packing
+    fractions 0.30-0.60, bidisperse radii, periodic boxes), stepped together in one handle
+    (per-system parameters and cell segments) and each held directly against the C oracle
+    run on that system alone: positions <= 1e-4 after 100 steps, forces <= 1e-3, and the
+    per-system energies of the final state to 1e-5 of the oracle's energies of that state."""
+    ws = W.c4(n_systems=96, seed=44, n_min=64, n_max=8192)
+    eng = Engine(3, [w.desc() for w in ws], K, skin=SKIN_OVER_RMAX * 0.7)
+    try:
+        eng.upload(pos=np.concatenate([w.pos for w in ws]), rad=np.concatenate([w.rad for w in ws]),
+                   mass=np.concatenate([w.mass for w in ws]), vel=np.concatenate([w.vel for w in ws]))
+        eng.step(steps)
+        out = eng.download()
+        e = eng.energy(per_system=True)
+    finally:
+        eng.close()
+    off = 0
+    worst = 0.0
+    for k, w in enumerate(ws):
+        pos, vel, frc = w.pos.copy(), w.vel.copy(), np.zeros_like(w.pos)
+        oracle.c_step(3, pos, vel, frc, w.rad, w.mass, dt=w.dt, steps=steps, acc64=True, **_okw(w))
+        sl = slice(off, off + w.N)
+        d = min_image_diff(out["pos_c"][sl], pos, w.box_size)
+        worst = max(worst, d)
+        assert d <= 1e-4, f"system {k} (N={w.N}): position error {d}"
+        assert force_err(out["force"][sl], frc) <= 1e-3, f"system {k}: force"
+        st = R.make_state(out["pos_c"][sl], vel=out["vel"][sl], rad=w.rad, mass=w.mass)
+        ref = R.compute_energy(st, osystem(w))
+        assert np.allclose(e[k][0], ref[0], rtol=1e-5, atol=1e-7), f"system {k}: contact energy"
+        assert np.allclose(e[k][2], ref[2], rtol=1e-5, atol=1e-7), f"system {k}: kinetic energy"
+        off += w.N
+    print(f"C4-style batch of {len(ws)} systems ({off} spheres): worst position error {worst:.2e}")
