@@ -93,7 +93,8 @@ typedef struct {
   int32_t chunk_steps;          /* steps per captured CUDA graph (<= 0: 50) */
   int32_t device;               /* CUDA device ordinal */
   int32_t neighbor_list;        /* Verlet list built at each re-sort: 0 = on (capacity from the
-                                   density), > 0 = on with this initial capacity, -1 = off */
+                                   density), > 0 = on with this initial capacity (rounded up
+                                   to a multiple of 4), -1 = off */
   int32_t graph_mode;           /* 0: CUDA graphs whose re-sort kernels sit in conditional nodes;
                                    systems of at most 32768 slots whose cooperative launch fits
                                    run each chunk as one many-step kernel in a while node;

@@ -495,7 +495,8 @@ int JdemHandle::plan_tiles() {
 // (Re)allocate the Verlet list for cap entries per slot (0: no list), one
 // cap x 32 block of entries per warp of slots.
 int JdemHandle::plan_list(int cap) {
-  cap = std::min(cap, kMaxListCap);
+  // a multiple of four entries per row: the force kernels read rows in batches of four
+  cap = std::min((cap + 3) / 4 * 4, kMaxListCap);
   const long long need = cap <= 0 ? 0 : ((P + 31) / 32) * 32LL * cap;
   if (cap > 0 && b.n_tiles > 0 && prepare_tbuild(tbuild_smem(b.tb_nst, b.tb_nv, b.tb_nrows)))
     return fail(JDEM_ERR_CUDA, "cannot raise shared memory for the list build");

@@ -151,9 +151,22 @@ struct ContactSum {
     return dsq;
   }
 
+  // add() for a list entry of a kernel without the GENERAL lookups (one pair
+  // constant, no bond or clump exclusions).  A padding entry (valid false:
+  // past the row's end, loaded with the slot's own position) is evaluated and
+  // discarded, so a row loop needs no branch per entry.  Returns the squared
+  // distance, like add().
+  __device__ __forceinline__ float add_plain(const float4& pj, bool may_wrap, bool valid) {
+    float dx, dy, dz;
+    const float dsq = pair_disp<DIM>(*sp, per && may_wrap, pi, pj, dx, dy, dz);
+    const float R = pi.w + pj.w;
+    if (valid && dsq < R * R * 1.000001f) contact(k0, dsq, R, pj.w, dx, dy, dz);
+    return dsq;
+  }
+
   // Contact force of one candidate, summed with the two-sum accumulator.
   __device__ __forceinline__ void contact(float k, float dsq, float R, float rj, float dx, float dy, float dz) {
-    float inv = dsq == 0.0f ? 0.0f : 1.0f / sqrtf(fmaxf(dsq, 1e-16f));
+    float inv = inv_norm(dsq);
     float rr = dsq * inv;
     float delta = R - rr;
     delta = delta > 0.0f ? delta : 0.0f;
@@ -269,7 +282,42 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
   const uint32_t tg = b.tag[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
   ContactSum<DIM, GENERAL, LAW> acc(b, sp, pi, tg, sel, t);
-  if (use_list && prune_out) {
+  // Rows without GENERAL lookups load four words and four positions per batch
+  // without per-entry branches: list rows hold a multiple of four entries, so
+  // the last batch's words stay inside the row, and its padding entries load
+  // the slot's own position and are discarded.
+  if (!GENERAL && use_list && prune_out) {
+    int m = 0;
+    for (int k = 0; k < n; k += 4) {
+      uint32_t e[4];
+      float4 q[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[u] = (uint32_t)__ldcs(&nb[(k + u) * stride]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = P[k + u < n ? (long long)(e[u] & kEntrySlot) : t];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const bool valid = k + u < n;
+        const float dsq = acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, valid);
+        const float rc = (pi.w + q[u].w + b.prune_skin) * 1.0001f;
+        if (valid && dsq < rc * rc) prune_out[(m++) * stride] = (int32_t)e[u];
+      }
+    }
+    *prune_cnt = m;
+  } else if (!GENERAL && use_list) {
+    for (int k = 0; k < n; k += 4) {
+      uint32_t e[4];
+      float4 q[4];
+      // list words are read once per step: streaming loads, so they do not
+      // displace the neighbours' positions from L1
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[u] = (uint32_t)__ldcs(&nb[(k + u) * stride]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = P[k + u < n ? (long long)(e[u] & kEntrySlot) : t];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, k + u < n);
+    }
+  } else if (use_list && prune_out) {
     // prune pass: the full row, keeping the entries the next passes need
     int m = 0;
     for (int k = 0; k < n; k += 4) {
@@ -294,8 +342,6 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
       uint32_t e[4];
       float4 q[4];
 #pragma unroll
-      // list words are read once per step: streaming loads, so they do not
-      // displace the neighbours' positions from L1 (79.5 -> 78.3 us at 1M)
       for (int u = 0; u < 4; ++u) e[u] = k + u < n ? (uint32_t)__ldcs(&nb[(k + u) * stride]) : 0u;
 #pragma unroll
       for (int u = 0; u < 4; ++u) q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
