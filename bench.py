@@ -188,11 +188,12 @@ def run_reference(args, rank, world):
 
 
 # -------------------------------------------------------------- ours
-def traffic_from_profile(workload, n, skin, pruning, prune_frac):
+def traffic_from_profile(workload, n, skin, pruning, prune_frac, prune_skin=0.0):
     """DRAM bytes per fused-kernel launch from the committed ncu captures
     (profiles/k_force_<workload>_traffic.json), when one was taken on this workload's
-    size, skin (within 5 %) and pruning setting: the inner- and prune-pass figures
-    weighted by the fraction of prune passes.  Returns (bytes, capture) or (None, None)."""
+    size, skin (within 5 %) and pruning setting (with pruning, the capture of the
+    nearest prune skin): the inner- and prune-pass figures weighted by the fraction
+    of prune passes.  Returns (bytes, capture) or (None, None)."""
     p = ROOT / "profiles" / f"k_force_{workload}_traffic.json"
     try:
         d = json.loads(p.read_text())
@@ -200,13 +201,14 @@ def traffic_from_profile(workload, n, skin, pruning, prune_frac):
         return None, None
     if d.get("n") != n:
         return None, None
-    for c in d.get("captures", []):
-        if abs(float(c["skin"]) - float(skin)) > 0.05 * float(skin) or bool(c["pruning"]) != bool(pruning):
-            continue
-        if pruning:
-            return prune_frac * c["prune_pass_bytes"] + (1.0 - prune_frac) * c["inner_pass_bytes"], c
-        return c["full_pass_bytes"], c
-    return None, None
+    cands = [c for c in d.get("captures", [])
+             if abs(float(c["skin"]) - float(skin)) <= 0.05 * float(skin) and bool(c["pruning"]) == bool(pruning)]
+    if not cands:
+        return None, None
+    if pruning:
+        c = min(cands, key=lambda c: abs(float(c.get("prune_skin", 0.0)) - float(prune_skin)))
+        return prune_frac * c["prune_pass_bytes"] + (1.0 - prune_frac) * c["inner_pass_bytes"], c
+    return cands[0]["full_pass_bytes"], cands[0]
 
 
 def peaks():
@@ -304,7 +306,8 @@ def run_ours(args, rank, world, dist):
     peak, peak_kind = peaks()
     achieved = B * w.N / (force_avg_ms * 1e-3) / 1e9
     pruning = stats["prunes"] > 0
-    traffic, capture = traffic_from_profile(args.workload, w.N, skin, pruning, prune_frac)
+    traffic, capture = traffic_from_profile(args.workload, w.N, skin, pruning, prune_frac,
+                                            prune_skin if prune_skin > 0 else skin / 3.0)
 
     # Secondary figures: the whole step against the same roofline; the step with the re-sort
     # traffic counted (a re-sort reads and writes each slot's record: position and velocity
@@ -394,8 +397,10 @@ def run_ours(args, rank, world, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "traffic_source": (f"ncu capture at skin {capture['skin']}, pruning "
-                                        f"{'on' if capture['pruning'] else 'off'}, weighted by this pass's "
-                                        f"prune fraction {prune_frac:.2f} ({capture['source']})")
+                                        f"{'on' if capture['pruning'] else 'off'}"
+                                        f"{', prune skin ' + str(capture['prune_skin']) if capture['pruning'] else ''}"
+                                        f", weighted by this pass's prune fraction {prune_frac:.2f} "
+                                        f"({capture['source']}; kernel: {capture.get('kernel', 'unknown')})")
                      if capture else "no ncu capture at this skin and pruning setting",
                      "kernel": ("k_force_small (8 lanes a slot), timed per launch: the timed region runs the "
                                 "same step inside cooperative many-step launches (k_multi)")
