@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--prune-skin", type=float, default=0.0,
                    help="inner-list margin of the Verlet-list dynamic pruning (0: skin / 3, < 0: off)")
     p.add_argument("--brick", type=int, default=0, help="particles per list-build brick (0: 240)")
+    p.add_argument("--force-block", type=int, default=0, help="threads per block of k_force (0: 128)")
+    p.add_argument("--small-lanes", type=int, default=0, help="lanes per slot at <= 32768 particles (0: 8)")
     p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -235,25 +237,27 @@ def run_ours(args, rank, world, dist):
     rmax = float(w.rad.max())
     tuning = None
     prune_skin, brick = args.prune_skin, args.brick
+    block, lanes = args.force_block, args.small_lanes
     if args.skin is not None:
         skin = args.skin
     elif args.no_tune:
         skin = autotune.default_skin(rmax)
     else:
-        def mk(skin, prune_skin, brick_particles):
-            return Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev,
-                          prune_skin=prune_skin, brick_particles=brick_particles)
+        def mk(**shape):
+            return Engine(w.dim, [w.desc()], young, chunk_steps=CHUNK, device=dev, **shape)
 
         best, timings = autotune.tune_shapes(mk, lambda e: e.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel),
                                              rmax, w.N, key=autotune.workload_key(w))
         skin, prune_skin, brick = best["skin"], best["prune_skin"], best["brick_particles"]
+        block, lanes = best["force_block"], best["small_lanes"]
         tuning = {"skin_over_rmax": round(skin / rmax, 3),
                   "prune_skin_over_skin": round(prune_skin / skin, 3) if prune_skin > 0 else "off",
-                  "brick_particles": brick,
+                  "brick_particles": brick, "force_block": block, "small_lanes": lanes,
                   "ms_per_step": {shape: {k: round(v * 1e3, 4) for k, v in t.items()}
-                                  for shape, t in timings.items()}}
+                                  for shape, t in timings.items() if t}}
+    shape_kw = dict(prune_skin=prune_skin, brick_particles=brick, force_block=block, small_lanes=lanes)
     eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev, graph_mode=args.graph_mode,
-                 prune_skin=prune_skin, brick_particles=brick)
+                 **shape_kw)
     eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -335,8 +339,7 @@ def run_ours(args, rank, world, dist):
         outb = {"pos_c": np.empty_like(w.pos), "vel": np.empty_like(w.vel), "force": np.empty_like(w.pos)}
         for a in list(host.values()) + list(outb.values()):
             host_register(a)
-        e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev,
-                         prune_skin=prune_skin, brick_particles=brick)
+        e2e_eng = Engine(w.dim, [w.desc()], young, skin=skin, chunk_steps=CHUNK, device=dev, **shape_kw)
         e2e_eng.upload(pos=host["pos"], rad=host["rad"], mass=host["mass"], vel=host["vel"])
         e2e_eng.step(K)  # the timed call sequence once: every graph it launches is captured here
         e2e_graphs = e2e_eng.stats()["graphs"]
@@ -391,6 +394,7 @@ def run_ours(args, rank, world, dist):
                    "graphs_captured_in_timed_region": graphs_captured_timed,
                    "prune_skin": "off" if prune_skin < 0 else (prune_skin or skin / 3.0),
                    "brick_particles": brick or 240,
+                   "force_block": block or 128, "small_lanes": lanes or 8,
                    "prunes_in_timed_region": stats["prunes"] - prunes_before,
                    "verlet_list": {"capacity": stats["list_capacity"], "tiles": stats["list_tiles"],
                                    "regrowths": stats["list_regrowths"]}},
@@ -415,7 +419,7 @@ def run_ours(args, rank, world, dist):
     }
     eng.close()
     if rank == 0 and world == 1 and not args.no_rollout:
-        line["rollout"] = run_rollout(args, w, young, skin, dev, torch, prune_skin=prune_skin, brick_particles=brick)
+        line["rollout"] = run_rollout(args, w, young, skin, dev, torch, **shape_kw)
     if rank == 0 and world == 1 and not args.no_batched:
         line["batched"] = run_batched(args, dev, flush, torch)
     if rank == 0 and world == 1 and not args.no_served:

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 10
+#define JDEM_ABI_VERSION 11
 
 enum {
   JDEM_OK = 0,
@@ -112,6 +112,12 @@ typedef struct {
                                    0: skin / 3; < 0: off (every step walks the full list) */
   int32_t brick_particles;      /* list build: particles per brick of cells staged in shared
                                    memory (<= 0: 240) */
+  int32_t force_block;          /* threads per block of the fused force kernel of handles above
+                                   32768 slots: 64, 128 or 256 (0: 128); results do not depend
+                                   on it */
+  int32_t small_lanes;          /* lanes sharing a slot in the force kernels of handles of at
+                                   most 32768 slots (per-step and many-step): 4, 8 or 16
+                                   (0: 8); the partial sums of a slot combine in lane order */
 } JdemConfig;
 
 /* Particle arrays in the reference layout.  Upload reads every field that is

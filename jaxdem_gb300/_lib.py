@@ -78,6 +78,8 @@ class Config(C.Structure):
         ("material_props", C.POINTER(C.c_float)),
         ("prune_skin", C.c_float),
         ("brick_particles", C.c_int32),
+        ("force_block", C.c_int32),
+        ("small_lanes", C.c_int32),
     ]
 
 
@@ -208,7 +210,7 @@ class Engine:
                  bond_width: int = 0, interact_same_bond_id: bool = False, chunk_steps: int = 50,
                  device: int = 0, neighbor_list=True, graph_mode: int = 0, force_law: str = "spring",
                  material_props: Optional[np.ndarray] = None, prune_skin: float = 0.0,
-                 brick_particles: int = 0):
+                 brick_particles: int = 0, force_block: int = 0, small_lanes: int = 0):
         """``young_eff`` is the (M, M) pair constant of ``force_law``: the spring's k,
         (4/3) E* for ``"hertz"`` (``forces.hertz_pair_constant``), or the damping ratio
         beta for ``"cundallstrack"``, which also takes ``material_props`` (M, 4)
@@ -263,6 +265,10 @@ class Engine:
         cfg.prune_skin = float(prune_skin)
         # particles per shared-memory brick of the list build (0: 240)
         cfg.brick_particles = int(brick_particles)
+        # threads per block of the fused force kernel above 32768 slots (0: 128), and
+        # lanes per slot of the small-system force kernels (0: 8)
+        cfg.force_block = int(force_block)
+        cfg.small_lanes = int(small_lanes)
         self.force_law = force_law
         self._props = None
         if material_props is not None:

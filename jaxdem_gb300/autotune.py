@@ -7,12 +7,18 @@
   margin but rebuilt from the full list more often (off, or a fraction of the
   skin);
 * brick size: particles per shared-memory brick of the list build (larger
-  bricks stage relatively fewer halo cells but fill fewer blocks).
+  bricks stage relatively fewer halo cells but fill fewer blocks);
+* force-kernel shape: threads per block of the fused force kernel above
+  32768 particles (64, 128 or 256: how many slots retire together against
+  the block-granular residency), or, at most 32768 particles, lanes sharing a
+  slot in the per-step and many-step force kernels (4, 8 or 16: a slot's row
+  split across more lanes shortens its chain of dependent loads but occupies
+  more threads and shuffles more partial sums).
 
 The best values depend on density, temperature and size, so they are
 measured: a coordinate search times a short chunk of steps on the actual
 system for each candidate of one shape at a time (skin, then prune skin, then
-brick size), keeping the fastest.  Results are cached per configuration class
+brick size, then the force-kernel shape), keeping the fastest.  Results are cached per configuration class
 (dimension, log2 particle bucket, density bucket, mean speed bucket) in a JSON
 file, so repeated runs of similar workloads skip the search.
 """
@@ -70,9 +76,13 @@ def workload_key(w) -> str:
     return config_key(w.dim, w.N, phi, vrms, w.domain)
 
 
-# prune skin as a fraction of the skin (-1: pruning off) and list-build brick sizes
+# prune skin as a fraction of the skin (-1: pruning off), list-build brick sizes,
+# force-kernel block sizes (above 32768 particles) and lanes per slot (at most 32768)
 PRUNE_CANDIDATES = (-1.0, 0.2, 1.0 / 3.0, 0.5)
 BRICK_CANDIDATES = (120, 240, 480)
+BLOCK_CANDIDATES = (64, 128, 256)
+LANE_CANDIDATES = (4, 8, 16)
+SMALL_SLOTS = 32768
 
 
 def _time_chunk(make_engine, upload, params, steps):
@@ -92,41 +102,51 @@ def _time_chunk(make_engine, upload, params, steps):
 
 def tune_shapes(make_engine: Callable[..., "object"], upload: Callable[["object"], None], rmax: float,
                 n_particles: int, key: Optional[str] = None, steps: int = 60, use_cache: bool = True) -> tuple[dict, dict]:
-    """Coordinate search over (skin, prune skin, brick size); returns (best, timings).
+    """Coordinate search over (skin, prune skin, brick size, force-kernel shape); returns (best, timings).
 
-    ``make_engine(skin=..., prune_skin=..., brick_particles=...)`` builds an engine and
-    ``upload(engine)`` loads the state.  ``best`` holds the three arguments; ``timings``
-    the seconds per step of every candidate, per shape.  The prune skin and brick size
-    only matter above 32768 particles (the fused list kernel and the brick build), so
-    smaller systems tune the skin alone.
+    ``make_engine(skin=..., prune_skin=..., brick_particles=..., force_block=..., small_lanes=...)``
+    builds an engine and ``upload(engine)`` loads the state.  ``best`` holds those five
+    arguments; ``timings`` the seconds per step of every candidate, per shape.  The prune
+    skin, brick size and block size only matter above 32768 particles (the fused list kernel
+    and the brick build); at most 32768 particles the skin and the lanes per slot are tuned.
     """
     cache = _load() if use_cache else {}
     ckey = None if key is None else "shapes:" + key
     if ckey is not None and ckey in cache:
         c = cache[ckey]
         return ({"skin": c["skin_rel"] * rmax, "prune_skin": c["prune_rel"] * c["skin_rel"] * rmax
-                 if c["prune_rel"] > 0 else -1.0, "brick_particles": int(c["brick"])}, c.get("timings", {}))
-    timings = {"skin": {}, "prune": {}, "brick": {}}
-    large = n_particles > 32768
-    base = {"prune_skin": 0.0, "brick_particles": 240}
+                 if c["prune_rel"] > 0 else -1.0, "brick_particles": int(c["brick"]),
+                 "force_block": int(c.get("block", 128)), "small_lanes": int(c.get("lanes", 8))},
+                c.get("timings", {}))
+    timings = {"skin": {}, "prune": {}, "brick": {}, "block": {}, "lanes": {}}
+    large = n_particles > SMALL_SLOTS
+    cur = {"prune_skin": 0.0, "brick_particles": 240, "force_block": 128, "small_lanes": 8}
     for c in CANDIDATES:
-        timings["skin"][str(c)] = _time_chunk(make_engine, upload, {"skin": c * rmax, **base}, steps)
+        timings["skin"][str(c)] = _time_chunk(make_engine, upload, {**cur, "skin": c * rmax}, steps)
     skin_rel = float(min(timings["skin"], key=timings["skin"].get))
-    prune_rel, brick = 1.0 / 3.0, 240
+    cur["skin"] = skin_rel * rmax
+    prune_rel = 1.0 / 3.0
     if large:
         for pr in PRUNE_CANDIDATES:
-            ps = -1.0 if pr < 0 else pr * skin_rel * rmax
-            timings["prune"][str(round(pr, 3))] = _time_chunk(
-                make_engine, upload, {"skin": skin_rel * rmax, "prune_skin": ps, "brick_particles": 240}, steps)
+            ps = -1.0 if pr < 0 else pr * cur["skin"]
+            timings["prune"][str(round(pr, 3))] = _time_chunk(make_engine, upload, {**cur, "prune_skin": ps}, steps)
         prune_rel = float(min(timings["prune"], key=timings["prune"].get))
-        ps = -1.0 if prune_rel < 0 else prune_rel * skin_rel * rmax
+        cur["prune_skin"] = -1.0 if prune_rel < 0 else prune_rel * cur["skin"]
         for bk in BRICK_CANDIDATES:
-            timings["brick"][str(bk)] = _time_chunk(
-                make_engine, upload, {"skin": skin_rel * rmax, "prune_skin": ps, "brick_particles": bk}, steps)
-        brick = int(min(timings["brick"], key=timings["brick"].get))
-    best = {"skin": skin_rel * rmax, "prune_skin": -1.0 if prune_rel < 0 else prune_rel * skin_rel * rmax,
-            "brick_particles": brick}
+            timings["brick"][str(bk)] = _time_chunk(make_engine, upload, {**cur, "brick_particles": bk}, steps)
+        cur["brick_particles"] = int(min(timings["brick"], key=timings["brick"].get))
+        for nt in BLOCK_CANDIDATES:
+            timings["block"][str(nt)] = _time_chunk(make_engine, upload, {**cur, "force_block": nt}, steps)
+        cur["force_block"] = int(min(timings["block"], key=timings["block"].get))
+    else:
+        for g in LANE_CANDIDATES:
+            timings["lanes"][str(g)] = _time_chunk(make_engine, upload, {**cur, "small_lanes": g}, steps)
+        cur["small_lanes"] = int(min(timings["lanes"], key=timings["lanes"].get))
+    best = {"skin": cur["skin"], "prune_skin": -1.0 if prune_rel < 0 else prune_rel * cur["skin"],
+            "brick_particles": cur["brick_particles"], "force_block": cur["force_block"],
+            "small_lanes": cur["small_lanes"]}
     if ckey is not None:
-        cache[ckey] = {"skin_rel": skin_rel, "prune_rel": prune_rel, "brick": brick, "timings": timings}
+        cache[ckey] = {"skin_rel": skin_rel, "prune_rel": prune_rel, "brick": cur["brick_particles"],
+                       "block": cur["force_block"], "lanes": cur["small_lanes"], "timings": timings}
         _store(cache)
     return best, timings

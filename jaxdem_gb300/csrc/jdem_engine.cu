@@ -156,6 +156,12 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   if (!std::isfinite(cfg->prune_skin)) return fail(JDEM_ERR_BAD_ARG, "config: prune_skin must be finite");
   prune_req = cfg->prune_skin;
   brick_tt = cfg->brick_particles > 0 ? (double)cfg->brick_particles : 240.0;
+  if (cfg->force_block != 0 && cfg->force_block != 64 && cfg->force_block != 128 && cfg->force_block != 256)
+    return fail(JDEM_ERR_BAD_ARG, "config: force_block must be 0, 64, 128 or 256");
+  if (cfg->small_lanes != 0 && cfg->small_lanes != 4 && cfg->small_lanes != 8 && cfg->small_lanes != 16)
+    return fail(JDEM_ERR_BAD_ARG, "config: small_lanes must be 0, 4, 8 or 16");
+  b.force_block = cfg->force_block ? cfg->force_block : 128;
+  b.small_lanes = cfg->small_lanes ? cfg->small_lanes : 8;
   int rc0 = set_systems(cfg->systems, S);
   if (rc0) return rc0;
   JDEM_CUDA_TRY(this, cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));

@@ -21,7 +21,10 @@ void launch_scan(const Bufs& b, cudaStream_t st);
 void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st);
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st);
 void launch_force(int dim, const Bufs& b, int mode, cudaStream_t st);
-// Systems of at most this many slots use k_force_small (8 lanes a slot).
+// Spheres without clumps or Cundall-Strack contacts (jdem_force2.cu, jdem_force3.cu).
+template <int DIM>
+void launch_force_dim(const Bufs& b, int mode, cudaStream_t st);
+// Systems of at most this many slots use k_force_small (Bufs.small_lanes lanes a slot).
 constexpr long long kSmallForceSlots = 32768;
 // Many steps per launch for small systems (jdem_multi.cu): whether the handle
 // qualifies (few enough slots to keep every block of the cooperative launch

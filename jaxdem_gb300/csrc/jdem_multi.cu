@@ -10,8 +10,8 @@
 // once when nothing is due), the list build and k_multi, which sets the
 // while condition.
 //
-// Each step is k_force_small's (8 lanes a slot, the same operations in the
-// same order) followed by k_fin's bound update, which every block evaluates
+// Each step is k_force_small's (Bufs.small_lanes lanes a slot, the same
+// operations in the same order) followed by k_fin's bound update, which every block evaluates
 // from the same inputs, so the trajectory is bit-identical to the launch per
 // step.  Positions written by other blocks in the previous step are read
 // with L2-coherent loads (never the read-only path).
@@ -23,9 +23,8 @@ namespace jdem {
 
 namespace {
 
-constexpr int kMultiG = 8;          // lanes per slot (as k_force_small)
 constexpr int kMultiT = 128;        // threads per block
-constexpr int kMultiE = 6;          // list entries a lane keeps in registers (row entries g, g + 8, ...; rows up to 48)
+constexpr int kMultiE = 6;          // list entries a lane keeps in registers (row entries g, g + G, ...; rows up to 6 G)
 constexpr int kMultiMaxSys = 8;     // systems of a handle that takes the many-step path
 constexpr unsigned int kBarrierSpins = 1u << 21;  // polls of the arrival count (about a second) before a barrier gives up
 
@@ -87,17 +86,16 @@ __device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& target,
 // ctl->steps_left = n: the steps of the captured chunk.
 __global__ void k_multi_init(Ctl* ctl, unsigned int n) { ctl->steps_left = n; }
 
-// Steps of one chunk until it ends or a re-sort is due.  A group of kMultiG
-// lanes owns slot t: the row entries, tag and system of the slot are loaded
+// Steps of one chunk until it ends or a re-sort is due.  A group of G lanes
+// (4, 8 or 16, as k_force_small's) owns slot t: the row entries, tag and system of the slot are loaded
 // once per launch (they change only at a re-sort), and the group's position
 // and the first lane's velocity stay in registers from step to step (the
 // group is their only writer), so a step's only dependent global loads are
 // the neighbours' positions, written by other blocks in the previous step and
 // read through L2.  The operations and their order are k_force_small's and
 // k_fin's.
-template <int DIM, bool GENERAL, int LAW>
+template <int DIM, bool GENERAL, int LAW, int G>
 __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalHandle hw) {
-  constexpr int G = kMultiG;
   Ctl* ctl = b.ctl;
   const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
   unsigned int left = ld_cg_u32(&ctl->steps_left);
@@ -238,17 +236,17 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
   }
 }
 
-template <int DIM, bool GENERAL, int LAW>
+template <int DIM, bool GENERAL, int LAW, int G>
 int multi_blocks_per_sm() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_multi<DIM, GENERAL, LAW>, kMultiT, 0) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_multi<DIM, GENERAL, LAW, G>, kMultiT, 0) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return nb;
 }
 
-template <int DIM, bool GENERAL, int LAW>
+template <int DIM, bool GENERAL, int LAW, int G>
 int launch_multi_t(const Bufs& b, cudaGraphConditionalHandle hw, unsigned int grid, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
@@ -260,10 +258,25 @@ int launch_multi_t(const Bufs& b, cudaGraphConditionalHandle hw, unsigned int gr
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_multi<DIM, GENERAL, LAW>, b, hw) == cudaSuccess ? 0 : 1;
+  return cudaLaunchKernelEx(&cfg, k_multi<DIM, GENERAL, LAW, G>, b, hw) == cudaSuccess ? 0 : 1;
 }
 
-unsigned int multi_grid(const Bufs& b) { return (unsigned int)((b.P * kMultiG + kMultiT - 1) / kMultiT); }
+unsigned int multi_grid(const Bufs& b) { return (unsigned int)((b.P * b.small_lanes + kMultiT - 1) / kMultiT); }
+
+// occupancy and launch of the instance for the handle's lane count
+template <int DIM, bool GENERAL, int LAW>
+int multi_blocks_per_sm_g(const Bufs& b) {
+  if (b.small_lanes == 4) return multi_blocks_per_sm<DIM, GENERAL, LAW, 4>();
+  if (b.small_lanes == 16) return multi_blocks_per_sm<DIM, GENERAL, LAW, 16>();
+  return multi_blocks_per_sm<DIM, GENERAL, LAW, 8>();
+}
+
+template <int DIM, bool GENERAL, int LAW>
+int launch_multi_g(const Bufs& b, cudaGraphConditionalHandle hw, unsigned int grid, cudaStream_t st) {
+  if (b.small_lanes == 4) return launch_multi_t<DIM, GENERAL, LAW, 4>(b, hw, grid, st);
+  if (b.small_lanes == 16) return launch_multi_t<DIM, GENERAL, LAW, 16>(b, hw, grid, st);
+  return launch_multi_t<DIM, GENERAL, LAW, 8>(b, hw, grid, st);
+}
 
 bool multi_general(const Bufs& b) { return b.n_mat > 1 || (b.bond_w > 0 && !b.interact_same_bond); }
 
@@ -281,11 +294,11 @@ bool multi_eligible(int dim, const Bufs& b, int device) {
   const bool gen = multi_general(b), hertz = b.law == LAW_HERTZ;
   int per_sm;
   if (dim == 3) {
-    per_sm = gen ? (hertz ? multi_blocks_per_sm<3, true, LAW_HERTZ>() : multi_blocks_per_sm<3, true, LAW_SPRING>())
-                 : (hertz ? multi_blocks_per_sm<3, false, LAW_HERTZ>() : multi_blocks_per_sm<3, false, LAW_SPRING>());
+    per_sm = gen ? (hertz ? multi_blocks_per_sm_g<3, true, LAW_HERTZ>(b) : multi_blocks_per_sm_g<3, true, LAW_SPRING>(b))
+                 : (hertz ? multi_blocks_per_sm_g<3, false, LAW_HERTZ>(b) : multi_blocks_per_sm_g<3, false, LAW_SPRING>(b));
   } else {
-    per_sm = gen ? (hertz ? multi_blocks_per_sm<2, true, LAW_HERTZ>() : multi_blocks_per_sm<2, true, LAW_SPRING>())
-                 : (hertz ? multi_blocks_per_sm<2, false, LAW_HERTZ>() : multi_blocks_per_sm<2, false, LAW_SPRING>());
+    per_sm = gen ? (hertz ? multi_blocks_per_sm_g<2, true, LAW_HERTZ>(b) : multi_blocks_per_sm_g<2, true, LAW_SPRING>(b))
+                 : (hertz ? multi_blocks_per_sm_g<2, false, LAW_HERTZ>(b) : multi_blocks_per_sm_g<2, false, LAW_SPRING>(b));
   }
   return (long long)per_sm * sms >= (long long)multi_grid(b);
 }
@@ -296,11 +309,11 @@ int launch_multi(int dim, const Bufs& b, cudaGraphConditionalHandle hw, cudaStre
   const unsigned int grid = multi_grid(b);
   const bool gen = multi_general(b), hertz = b.law == LAW_HERTZ;
   if (dim == 3) {
-    if (gen) return hertz ? launch_multi_t<3, true, LAW_HERTZ>(b, hw, grid, st) : launch_multi_t<3, true, LAW_SPRING>(b, hw, grid, st);
-    return hertz ? launch_multi_t<3, false, LAW_HERTZ>(b, hw, grid, st) : launch_multi_t<3, false, LAW_SPRING>(b, hw, grid, st);
+    if (gen) return hertz ? launch_multi_g<3, true, LAW_HERTZ>(b, hw, grid, st) : launch_multi_g<3, true, LAW_SPRING>(b, hw, grid, st);
+    return hertz ? launch_multi_g<3, false, LAW_HERTZ>(b, hw, grid, st) : launch_multi_g<3, false, LAW_SPRING>(b, hw, grid, st);
   }
-  if (gen) return hertz ? launch_multi_t<2, true, LAW_HERTZ>(b, hw, grid, st) : launch_multi_t<2, true, LAW_SPRING>(b, hw, grid, st);
-  return hertz ? launch_multi_t<2, false, LAW_HERTZ>(b, hw, grid, st) : launch_multi_t<2, false, LAW_SPRING>(b, hw, grid, st);
+  if (gen) return hertz ? launch_multi_g<2, true, LAW_HERTZ>(b, hw, grid, st) : launch_multi_g<2, true, LAW_SPRING>(b, hw, grid, st);
+  return hertz ? launch_multi_g<2, false, LAW_HERTZ>(b, hw, grid, st) : launch_multi_g<2, false, LAW_SPRING>(b, hw, grid, st);
 }
 
 }  // namespace jdem

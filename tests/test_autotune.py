@@ -17,6 +17,8 @@ def test_coordinate_search_picks_each_shape_and_caches(monkeypatch, tmp_path):
         if ps > 0:
             cost -= 0.02 * (1.0 - abs(ps / skin - 0.2))  # pruning at 0.2 x skin is best
         cost += 0.001 * abs(bk - 480) / 480
+        cost += 0.0005 * (params["force_block"] != 64)
+        assert params["small_lanes"] == 8  # not tuned above 32768 particles
         return cost
 
     monkeypatch.setattr(autotune, "_time_chunk", fake_time)
@@ -25,20 +27,27 @@ def test_coordinate_search_picks_each_shape_and_caches(monkeypatch, tmp_path):
     assert abs(best["skin"] - 0.65 * 0.7) < 1e-9
     assert abs(best["prune_skin"] - 0.2 * best["skin"]) < 1e-9
     assert best["brick_particles"] == 480
+    assert best["force_block"] == 64 and best["small_lanes"] == 8
     n = len(calls)
-    assert n == len(autotune.CANDIDATES) + len(autotune.PRUNE_CANDIDATES) + len(autotune.BRICK_CANDIDATES)
-    assert set(timings) == {"skin", "prune", "brick"}
+    assert n == (len(autotune.CANDIDATES) + len(autotune.PRUNE_CANDIDATES) + len(autotune.BRICK_CANDIDATES)
+                 + len(autotune.BLOCK_CANDIDATES))
+    # each shape is searched with the best values found before it
+    assert all(c["brick_particles"] == 480 for c in calls[-len(autotune.BLOCK_CANDIDATES):])
+    assert set(timings) == {"skin", "prune", "brick", "block", "lanes"} and timings["lanes"] == {}
     cached = json.loads((tmp_path / "tune.json").read_text())["shapes:k"]
-    assert cached["brick"] == 480
+    assert cached["brick"] == 480 and cached["block"] == 64
     # a second call is served from the cache
     best2, _ = autotune.tune_shapes(None, None, 0.7, 1 << 20, key="k")
     assert len(calls) == n and best2 == best
 
 
-def test_small_systems_tune_the_skin_only(monkeypatch, tmp_path):
+def test_small_systems_tune_the_skin_and_lanes_per_slot(monkeypatch, tmp_path):
     seen = []
-    monkeypatch.setattr(autotune, "_time_chunk", lambda mk, up, p, s: seen.append(p) or p["skin"])
+    monkeypatch.setattr(autotune, "_time_chunk",
+                        lambda mk, up, p, s: seen.append(p) or p["skin"] + 0.001 * abs(p["small_lanes"] - 16))
     monkeypatch.setattr(autotune, "CACHE", tmp_path / "tune.json")
     best, timings = autotune.tune_shapes(None, None, 0.5, 4096, key=None)
-    assert len(seen) == len(autotune.CANDIDATES)
-    assert best["skin"] == min(autotune.CANDIDATES) * 0.5 and timings["prune"] == {}
+    assert len(seen) == len(autotune.CANDIDATES) + len(autotune.LANE_CANDIDATES)
+    assert best["skin"] == min(autotune.CANDIDATES) * 0.5 and timings["prune"] == {} and timings["block"] == {}
+    assert best["small_lanes"] == 16 and best["force_block"] == 128
+    assert all(p["skin"] == best["skin"] for p in seen[-len(autotune.LANE_CANDIDATES):])
