@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 11
+#define JDEM_ABI_VERSION 12
 
 enum {
   JDEM_OK = 0,
@@ -294,6 +294,23 @@ int jdem_download_device_async(JdemHandle* h, JdemHostState* dev);
  * incomplete and the handle runs later steps one launch per step.  For tests of the
  * timeout path; normal use never calls it. */
 int jdem_set_barrier_limit(JdemHandle* h, uint32_t spins, uint32_t extra_arrivals);
+
+/* One integrator stage on caller-owned device buffers, for callers that run the
+ * reference's stage order themselves through the split factory types
+ * (Integrator.step_before_force / step_after_force, integrators/__init__.py:51-91):
+ * stage 0 = step_before_force, 1 = step_after_force of the linear integrator
+ * `linear` (JDEM_LIN_*: VelocityVerlet velocity_verlet.py:29-95, DirectEuler
+ * direct_euler.py:30-66) and of the rotation integrator `rotation` (JDEM_ROT_*:
+ * VelocityVerletSpiral velocity_verlet_spiral.py:36-180, Spiral spiral.py:56-144);
+ * either may be NONE.  pos_c, vel, force: n*dim floats; mass: n; fixed: n bytes
+ * or NULL (every particle free); q: n*4 floats (w, x, y, z), 16-byte aligned;
+ * ang_vel, torque, inertia: n*(dim == 3 ? 3 : 1) floats (lab frame; rotation
+ * only).  pos_c, vel, q and ang_vel are updated in place with the fused step's
+ * arithmetic; work is queued on `stream` (NULL: the default stream), nothing is
+ * allocated and nothing waits. */
+int jdem_integrate(int32_t dim, int64_t n, int32_t linear, int32_t rotation, int32_t stage, float dt,
+                   float* pos_c, float* vel, const float* force, const float* mass, const uint8_t* fixed,
+                   float* q, float* ang_vel, const float* torque, const float* inertia, void* stream);
 
 /* Contact forces of one sphere system from caller-owned device buffers, without
  * allocating device memory.  No counterpart in the reference: it exists for callers

@@ -168,6 +168,8 @@ _PROTOS = [
     ("jdem_download_device_async", [C.c_void_p, C.POINTER(HostState)], C.c_int),
     ("jdem_host_register", [C.c_void_p, C.c_size_t], C.c_int),
     ("jdem_host_unregister", [C.c_void_p], C.c_int),
+    ("jdem_integrate", [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_float] + [C.c_void_p] * 10,
+     C.c_int),
 ]
 
 EXPORTED = [p[0] for p in _PROTOS]

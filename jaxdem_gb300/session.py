@@ -21,7 +21,7 @@ from typing import Any, Callable, Optional
 
 import numpy as np
 
-from ._lib import DOMAIN, LINEAR, ROTATION, Engine
+from ._lib import DOMAIN, LINEAR, ROTATION, Engine, JdemError, load
 from .factory import _normalize_key
 from .state import Quaternion, State
 
@@ -403,3 +403,47 @@ def contacts(state: State, system) -> np.ndarray:
     eng = engine_for(state, system)
     upload(eng, state)
     return eng.contacts()
+
+
+
+def integrate_stage(state: State, system, linear: str, rotation: str, stage: int):
+    """One integrator stage on the GPU (``jdem_integrate``): ``step_before_force``
+    (stage 0) or ``step_after_force`` (stage 1) of the linear integrator ``linear``
+    and the rotation integrator ``rotation`` (either may be ``""``), as the split
+    factory types call them (``integrators/__init__.py:51-91``).  Returns a new state
+    and the system, the reference's functional contract.  Batched states take each
+    system's own ``dt``.  Device buffers are torch tensors on the current device and
+    the work is queued on torch's current stream."""
+    import torch
+
+    lin, rot = LINEAR[linear], ROTATION[rotation]
+    st = state.copy()
+    if (lin == 0 and rot == 0) or (lin == LINEAR["euler"] and rot == 0 and stage == 0):
+        return st, system
+    lib = load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    B, N, d = state.batch_size, state.N, state.dim
+    ad = 3 if d == 3 else 1
+    dts = np.broadcast_to(np.asarray(system.dt, np.float32).reshape(-1), (B,))
+
+    def dev_t(a, tail, dtype=np.float32):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype).reshape((B, N) + tail))).to(dev)
+
+    pos, vel, frc = dev_t(st.pos_c, (d,)), dev_t(st.vel, (d,)), dev_t(st.force, (d,))
+    mass, fixed = dev_t(st.mass, ()), dev_t(st.fixed, (), np.uint8)
+    q, w = dev_t(st.q.as_array(), (4,)), dev_t(st.ang_vel, (ad,))
+    tq, inertia = dev_t(st.torque, (ad,)), dev_t(st.inertia, (ad,))
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for b in range(B):
+        rc = lib.jdem_integrate(d, N, lin, rot, int(stage), float(dts[b]), pos[b].data_ptr(), vel[b].data_ptr(),
+                                frc[b].data_ptr(), mass[b].data_ptr(), fixed[b].data_ptr(), q[b].data_ptr(),
+                                w[b].data_ptr(), tq[b].data_ptr(), inertia[b].data_ptr(), stream)
+        if rc != 0:
+            raise JdemError(rc, "jdem_integrate failed")
+    torch.cuda.current_stream(dev).synchronize()
+    shp = state.pos_c.shape
+    st.pos_c = pos.cpu().numpy().reshape(shp)
+    st.vel = vel.cpu().numpy().reshape(shp)
+    st.q = Quaternion.from_array(q.cpu().numpy().reshape((*shp[:-1], 4)))
+    st.ang_vel = w.cpu().numpy().reshape(state.ang_vel.shape)
+    return st, system

@@ -62,6 +62,13 @@ def test_null_arguments_are_rejected_without_device_work(lib):
     assert lib.jdem_step(None, 1) == 1
     assert lib.jdem_create(None, None) == 1
     assert lib.jdem_last_error(None) == b"null handle"
+    # integrator stages: argument checks come before any device work
+    args = [None] * 10
+    assert lib.jdem_integrate(4, 8, 1, 0, 0, 1e-3, *args) == 1  # dim
+    assert lib.jdem_integrate(3, 8, 1, 0, 2, 1e-3, *args) == 1  # stage
+    assert lib.jdem_integrate(3, 8, 3, 0, 0, 1e-3, *args) == 1  # linear kind
+    assert lib.jdem_integrate(3, 8, 1, 0, 0, 1e-3, *args) == 1  # missing arrays
+    assert lib.jdem_integrate(3, 0, 1, 1, 0, 1e-3, *args) == 0  # nothing to do
 
 
 def test_config_struct_layout_matches_header(lib):
