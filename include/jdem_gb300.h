@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JDEM_ABI_VERSION 12
+#define JDEM_ABI_VERSION 13
 
 enum {
   JDEM_OK = 0,
@@ -311,6 +311,29 @@ int jdem_set_barrier_limit(JdemHandle* h, uint32_t spins, uint32_t extra_arrival
 int jdem_integrate(int32_t dim, int64_t n, int32_t linear, int32_t rotation, int32_t stage, float dt,
                    float* pos_c, float* vel, const float* force, const float* mass, const uint8_t* fixed,
                    float* q, float* ang_vel, const float* torque, const float* inertia, void* stream);
+
+/* Domain.apply of one sphere system (system.py:60-82, first stage) on caller-owned
+ * device buffers: JDEM_DOMAIN_PERIODIC has nothing to do (domains/__init__.py:123-189);
+ * JDEM_DOMAIN_REFLECT reflects spheres off the walls with the Verlet time-of-collision
+ * correction (reflect.py:99-299, _toc.py:11-94), using the previous step's force, and
+ * renormalises q when given (reflect.py:291-294); JDEM_DOMAIN_FREE writes the bounding
+ * box of pos_c -+ (|pos_p| + rad) to box_out / anchor_out (host arrays of dim floats,
+ * free.py:40-63; pos_p may be NULL) and waits for it on the host.  box_size and anchor
+ * are host arrays of dim floats; fixed may be NULL; q is 16-byte aligned or NULL.
+ * Rigid clumps take System.step (jdem_step). */
+int jdem_domain_apply(int32_t dim, int64_t n, int32_t domain, float dt, float restitution,
+                      const float* box_size, const float* anchor, float* pos_c, float* vel, const float* force,
+                      const float* rad, const float* mass, const uint8_t* fixed, const float* pos_p, float* q,
+                      float* box_out, float* anchor_out, void* stream);
+
+/* ForceManager.apply of one sphere system on caller-owned device buffers
+ * (force_manager.py:338-425 with every sphere its own body): force += external_force,
+ * then + external_force_com + gravity * mass; torque += external_torque.  gravity is a
+ * host array of dim floats; the external arrays may be NULL (zero); torque may be NULL
+ * (not updated).  Queued on `stream`, nothing waits. */
+int jdem_force_manager_apply(int32_t dim, int64_t n, const float* gravity, float* force, float* torque,
+                             const float* external_force, const float* external_force_com,
+                             const float* external_torque, const float* mass, void* stream);
 
 /* Contact forces of one sphere system from caller-owned device buffers, without
  * allocating device memory.  No counterpart in the reference: it exists for callers

@@ -170,6 +170,8 @@ _PROTOS = [
     ("jdem_host_unregister", [C.c_void_p], C.c_int),
     ("jdem_integrate", [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_float] + [C.c_void_p] * 10,
      C.c_int),
+    ("jdem_domain_apply", [C.c_int32, C.c_int64, C.c_int32, C.c_float, C.c_float] + [C.c_void_p] * 13, C.c_int),
+    ("jdem_force_manager_apply", [C.c_int32, C.c_int64] + [C.c_void_p] * 8, C.c_int),
 ]
 
 EXPORTED = [p[0] for p in _PROTOS]

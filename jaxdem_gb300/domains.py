@@ -48,11 +48,23 @@ class Domain(Factory):
     def shift(state, system):
         return state, system
 
+    @staticmethod
+    def apply(state, system):
+        """``Domain.apply`` (``domains/__init__.py:123-189``): the base domain leaves
+        state and system unchanged."""
+        return state, system
+
 
 @Domain.register("free")
 @dataclass
 class FreeDomain(Domain):
-    pass
+    @staticmethod
+    def apply(state, system):
+        """``FreeDomain.apply`` (``free.py:40-63``): box and anchor follow the
+        particles' bounding box, reduced on the GPU."""
+        from . import session
+
+        return session.domain_apply(state, system)
 
 
 @Domain.register("periodic")
@@ -90,3 +102,11 @@ class ReflectDomain(Domain):
             raise ValueError(f"restitution_coefficient must be in (0, 1], got {restitution_coefficient}.")
         return super().Create(dim, box_size=box_size, anchor=anchor,
                               restitution_coefficient=F32(restitution_coefficient), **kw)
+
+    @staticmethod
+    def apply(state, system):
+        """``ReflectDomain.apply`` (``reflect.py:99-299``) for spheres on the GPU: wall
+        impulses with the Verlet time-of-collision correction."""
+        from . import session
+
+        return session.domain_apply(state, system)

@@ -120,6 +120,15 @@ class ForceManager:
                             is_com_force=tuple(bool(f[-1]) if isinstance(f[-1], bool) else False for f in funcs))
 
     @staticmethod
+    def apply(state, system):
+        """``ForceManager.apply`` (``force_manager.py:338-425``) for spheres on the GPU:
+        external forces and gravity join the contact force; the returned system's external
+        buffers are cleared."""
+        from . import session
+
+        return session.force_manager_apply(state, system)
+
+    @staticmethod
     def add_force(state, system, force, *, is_com: bool = False):
         """Accumulate a one-step external force (``force_manager.py:192-``)."""
         fm = system.force_manager

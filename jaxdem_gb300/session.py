@@ -406,6 +406,110 @@ def contacts(state: State, system) -> np.ndarray:
 
 
 
+class _DeviceArrays:
+    """Torch tensors on the current device for the stage entry points: one (B, N, ...)
+    float32 (or given dtype) tensor per state field, and the current stream."""
+
+    def __init__(self, state: State):
+        import torch
+
+        self.torch = torch
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.B, self.N, self.d = state.batch_size, state.N, state.dim
+        self.stream = torch.cuda.current_stream(self.dev).cuda_stream
+
+    def put(self, a, tail, dtype=np.float32):
+        arr = np.ascontiguousarray(np.asarray(a, dtype).reshape((self.B, self.N) + tail))
+        return self.torch.from_numpy(arr).to(self.dev)
+
+    def finish(self):
+        self.torch.cuda.current_stream(self.dev).synchronize()
+
+
+def _per_system(x, B: int, tail: tuple) -> np.ndarray:
+    return np.broadcast_to(np.asarray(x, np.float32), (B, *tail) if tail else (B,)).reshape((B, *tail))
+
+
+def domain_apply(state: State, system):
+    """``Domain.apply`` (first stage of ``_step_once``, ``system.py:60-82``) on the GPU
+    (``jdem_domain_apply``): reflecting walls move and kick spheres, the free domain's box
+    follows the particles, the periodic domain does nothing.  Returns a new state and
+    system (the reference's functional contract)."""
+    dom = system.domain
+    key = dom.type_name
+    if key not in DOMAIN:
+        raise NotImplementedError(f"domain {key!r} is outside the GB300 hot path")
+    st = state.copy()
+    if key == "periodic" or state.N == 0:
+        return st, system
+    if _has_clumps(state):
+        raise NotImplementedError("Domain.apply of rigid clumps runs inside System.step")
+    lib = load()
+    A = _DeviceArrays(state)
+    B, N, d = A.B, A.N, A.d
+    box = _per_system(dom.box_size, B, (d,))
+    anc = _per_system(dom.anchor, B, (d,))
+    dts = _per_system(system.dt, B, ())
+    rest = _per_system(getattr(dom, "restitution_coefficient", 1.0), B, ())
+    pos, vel, frc = A.put(st.pos_c, (d,)), A.put(st.vel, (d,)), A.put(st.force, (d,))
+    rad, mass, fixed = A.put(st.rad, ()), A.put(st.mass, ()), A.put(st.fixed, (), np.uint8)
+    q = A.put(st.q.as_array(), (4,))
+    box_out, anc_out = np.zeros((B, d), F32), np.zeros((B, d), F32)
+    for b in range(B):
+        bx, an = np.ascontiguousarray(box[b]), np.ascontiguousarray(anc[b])
+        rc = lib.jdem_domain_apply(d, N, DOMAIN[key], float(dts[b]), float(rest[b]), bx.ctypes.data, an.ctypes.data,
+                                   pos[b].data_ptr(), vel[b].data_ptr(), frc[b].data_ptr(), rad[b].data_ptr(),
+                                   mass[b].data_ptr(), fixed[b].data_ptr(), None, q[b].data_ptr(),
+                                   box_out[b].ctypes.data, anc_out[b].ctypes.data, A.stream)
+        if rc != 0:
+            raise JdemError(rc, "jdem_domain_apply failed")
+    A.finish()
+    if key == "free":
+        shp = np.shape(dom.box_size)
+        nb, na = box_out.reshape(shp), anc_out.reshape(shp)
+        return st, dataclasses.replace(system, domain=dataclasses.replace(dom, box_size=nb, anchor=na))
+    shp = state.pos_c.shape
+    st.pos_c = pos.cpu().numpy().reshape(shp)
+    st.vel = vel.cpu().numpy().reshape(shp)
+    st.q = Quaternion.from_array(q.cpu().numpy().reshape((*shp[:-1], 4)))
+    return st, system
+
+
+def force_manager_apply(state: State, system):
+    """``ForceManager.apply`` (``force_manager.py:338-425``) for spheres on the GPU
+    (``jdem_force_manager_apply``): the external buffers and gravity join the contact
+    force and torque, and the returned system's external buffers are cleared."""
+    fm = system.force_manager
+    if getattr(fm, "force_functions", ()):
+        raise NotImplementedError("user force functions are outside the GB300 hot path")
+    st = state.copy()
+    if state.N == 0:
+        return st, system
+    if _has_clumps(state):
+        raise NotImplementedError("ForceManager.apply of rigid clumps runs inside System.step")
+    lib = load()
+    A = _DeviceArrays(state)
+    B, N, d = A.B, A.N, A.d
+    ad = 3 if d == 3 else 1
+    grav = _per_system(fm.gravity, B, (d,))
+    frc, tq, mass = A.put(st.force, (d,)), A.put(st.torque, (ad,)), A.put(st.mass, ())
+    ef, efc, et = A.put(fm.external_force, (d,)), A.put(fm.external_force_com, (d,)), A.put(fm.external_torque, (ad,))
+    for b in range(B):
+        g = np.ascontiguousarray(grav[b])
+        rc = lib.jdem_force_manager_apply(d, N, g.ctypes.data, frc[b].data_ptr(), tq[b].data_ptr(), ef[b].data_ptr(),
+                                          efc[b].data_ptr(), et[b].data_ptr(), mass[b].data_ptr(), A.stream)
+        if rc != 0:
+            raise JdemError(rc, "jdem_force_manager_apply failed")
+    A.finish()
+    shp = state.pos_c.shape
+    st.force = frc.cpu().numpy().reshape(shp)
+    st.torque = tq.cpu().numpy().reshape(state.torque.shape)
+    nfm = dataclasses.replace(fm, external_force=np.zeros_like(fm.external_force),
+                              external_force_com=np.zeros_like(fm.external_force_com),
+                              external_torque=np.zeros_like(fm.external_torque))
+    return st, dataclasses.replace(system, force_manager=nfm)
+
+
 def integrate_stage(state: State, system, linear: str, rotation: str, stage: int):
     """One integrator stage on the GPU (``jdem_integrate``): ``step_before_force``
     (stage 0) or ``step_after_force`` (stage 1) of the linear integrator ``linear``
@@ -414,33 +518,27 @@ def integrate_stage(state: State, system, linear: str, rotation: str, stage: int
     and the system, the reference's functional contract.  Batched states take each
     system's own ``dt``.  Device buffers are torch tensors on the current device and
     the work is queued on torch's current stream."""
-    import torch
-
     lin, rot = LINEAR[linear], ROTATION[rotation]
     st = state.copy()
     if (lin == 0 and rot == 0) or (lin == LINEAR["euler"] and rot == 0 and stage == 0):
         return st, system
     lib = load()
-    dev = torch.device("cuda", torch.cuda.current_device())
-    B, N, d = state.batch_size, state.N, state.dim
+    A = _DeviceArrays(state)
+    B, N, d = A.B, A.N, A.d
     ad = 3 if d == 3 else 1
-    dts = np.broadcast_to(np.asarray(system.dt, np.float32).reshape(-1), (B,))
-
-    def dev_t(a, tail, dtype=np.float32):
-        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype).reshape((B, N) + tail))).to(dev)
-
-    pos, vel, frc = dev_t(st.pos_c, (d,)), dev_t(st.vel, (d,)), dev_t(st.force, (d,))
-    mass, fixed = dev_t(st.mass, ()), dev_t(st.fixed, (), np.uint8)
-    q, w = dev_t(st.q.as_array(), (4,)), dev_t(st.ang_vel, (ad,))
-    tq, inertia = dev_t(st.torque, (ad,)), dev_t(st.inertia, (ad,))
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    dts = _per_system(system.dt, B, ())
+    pos, vel, frc = A.put(st.pos_c, (d,)), A.put(st.vel, (d,)), A.put(st.force, (d,))
+    mass, fixed = A.put(st.mass, ()), A.put(st.fixed, (), np.uint8)
+    q, w = A.put(st.q.as_array(), (4,)), A.put(st.ang_vel, (ad,))
+    tq, inertia = A.put(st.torque, (ad,)), A.put(st.inertia, (ad,))
+    stream = A.stream
     for b in range(B):
         rc = lib.jdem_integrate(d, N, lin, rot, int(stage), float(dts[b]), pos[b].data_ptr(), vel[b].data_ptr(),
                                 frc[b].data_ptr(), mass[b].data_ptr(), fixed[b].data_ptr(), q[b].data_ptr(),
                                 w[b].data_ptr(), tq[b].data_ptr(), inertia[b].data_ptr(), stream)
         if rc != 0:
             raise JdemError(rc, "jdem_integrate failed")
-    torch.cuda.current_stream(dev).synchronize()
+    A.finish()
     shp = state.pos_c.shape
     st.pos_c = pos.cpu().numpy().reshape(shp)
     st.vel = vel.cpu().numpy().reshape(shp)
