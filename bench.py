@@ -213,6 +213,16 @@ def traffic_from_profile(workload, n, skin, pruning, prune_frac, prune_skin=0.0)
     return cands[0]["full_pass_bytes"], cands[0]
 
 
+def l2_hit_from(capture, pruning, prune_frac):
+    """L2 sector hit rate (lts__t_sector_hit_rate.pct) of the same capture as the traffic,
+    the two passes weighted like the bytes; None when the capture did not record it."""
+    if not capture:
+        return None
+    if pruning and "inner_pass_l2_hit_pct" in capture:
+        return prune_frac * capture["prune_pass_l2_hit_pct"] + (1.0 - prune_frac) * capture["inner_pass_l2_hit_pct"]
+    return capture.get("full_pass_l2_hit_pct")
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -410,6 +420,7 @@ def run_ours(args, rank, world, dist):
                                 "same step inside cooperative many-step launches (k_multi)")
                      if stats.get("many_step") else "k_force (fused force + integrate)",
                      "bytes_per_unit": B,
+                     "l2_hit_pct": l2_hit_from(capture, pruning, prune_frac),
                      "avg_launch_ms": force_avg_ms, **step_roof},
         "contacts": contacts,
         "cpu_baseline": cpu,
@@ -417,6 +428,15 @@ def run_ours(args, rank, world, dist):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if stats.get("many_step"):
+        # a small system is bound by launch and dependent-load latency, not by HBM: the
+        # step's time beside the same step launched kernel by kernel and its force kernel
+        line["latency"] = {"us_per_step": total_ms / K * 1e3,
+                           "force_kernel_us": force_avg_ms * 1e3,
+                           "resorts_per_step": rebuilds_timed / K,
+                           "note": ("us_per_step: cooperative many-step launches (one grid barrier a "
+                                    "step); force_kernel_us: the same step's force kernel launched alone "
+                                    "(CUDA events around each launch), one chain of dependent loads")}
     eng.close()
     if rank == 0 and world == 1 and not args.no_rollout:
         line["rollout"] = run_rollout(args, w, young, skin, dev, torch, **shape_kw)
