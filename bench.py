@@ -495,11 +495,36 @@ def run_batched(args, dev, flush, torch, n_systems=4096, steps=1000):
     from jaxdem_gb300._lib import Engine
     from jaxdem_gb300.batch import BatchedSystems
 
+    from jaxdem_gb300 import autotune
+
     ws = W.c4(n_systems=n_systems)
     total = sum(w.N for w in ws)
     rmax = max(float(w.rad.max()) for w in ws)
-    skin = args.skin if args.skin is not None else 0.65 * rmax
-    bs = BatchedSystems(ws, skin=skin, chunk_steps=CHUNK, device=dev)
+    shapes, tuning = {}, None
+    if args.skin is not None or args.no_tune:
+        skin = args.skin if args.skin is not None else autotune.default_skin(rmax)
+    else:
+        from jaxdem_gb300.batch import tune_key
+
+        key = tune_key(ws)
+
+        def mk(skin, **shape):
+            return BatchedSystems(ws, skin=skin, chunk_steps=CHUNK, device=dev, **shape).engine
+
+        def up(eng):
+            cat = lambda k: np.concatenate([getattr(w, k) for w in ws])  # noqa: E731
+            eng.upload(pos=cat("pos"), rad=cat("rad"), mass=cat("mass"), vel=cat("vel"))
+
+        best, timings = autotune.tune_shapes(mk, up, rmax, total, key=key, steps=CHUNK)
+        skin = best.pop("skin")
+        shapes = best
+        ps = shapes["prune_skin"]
+        tuning = {"skin_over_rmax": round(skin / rmax, 3),
+                  "prune_skin_over_skin": round(ps / skin, 3) if ps > 0 else "off",
+                  "brick_particles": shapes["brick_particles"], "force_block": shapes["force_block"],
+                  "small_lanes": shapes["small_lanes"],
+                  "ms_per_step": {sh: {k: round(v * 1e3, 4) for k, v in t.items()} for sh, t in timings.items() if t}}
+    bs = BatchedSystems(ws, skin=skin, chunk_steps=CHUNK, device=dev, **shapes)
     bs.upload()
     bs.step(CHUNK)  # warm-up: capture, first re-sort
     stream = torch.cuda.ExternalStream(bs.engine.stream(), device=dev)
@@ -534,7 +559,7 @@ def run_batched(args, dev, flush, torch, n_systems=4096, steps=1000):
     plain = ps_sum / t_sum
     return {"workload": f"{n_systems} periodic 3D systems, N~logU[64,16384] (total {total}), phi~U[0.3,0.6], "
                         f"r 0.5/0.7, dt=1e-3, {steps} steps in {CHUNK}-step graph chunks",
-            "value": batched, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+            "value": batched, "unit": "particle-steps/s", "ms_per_step": ms / steps, "autotune": tuning,
             "plain_looped": plain, "batched_over_plain": batched / plain,
             "plain_sample": f"{len(sample)} of {n_systems} systems stepped one at a time ({p_steps} steps each, "
                             f"one handle and graph per system), throughput = sum(N*steps)/sum(time)"}

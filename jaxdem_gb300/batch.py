@@ -30,7 +30,9 @@ class BatchedSystems:
     """
 
     def __init__(self, workloads: Sequence[Workload], young: float = K_SPRING, skin: Optional[float] = None,
-                 chunk_steps: int = 50, device: int = 0, neighbor_list=True):
+                 chunk_steps: int = 50, device: int = 0, neighbor_list=True, **shapes):
+        """``shapes`` are the engine's tunable shapes (``prune_skin``, ``brick_particles``,
+        ``force_block``, ``small_lanes``; see ``autotune.tune_shapes``)."""
         if not workloads:
             raise ValueError("no systems")
         dims = {w.dim for w in workloads}
@@ -43,7 +45,7 @@ class BatchedSystems:
         rmax = max(float(w.rad.max()) for w in workloads if w.N)
         self.skin = float(skin) if skin is not None else autotune.default_skin(rmax)
         self.engine = Engine(self.dim, [w.desc() for w in workloads], np.array([[young]], F32), skin=self.skin,
-                             chunk_steps=chunk_steps, device=device, neighbor_list=neighbor_list)
+                             chunk_steps=chunk_steps, device=device, neighbor_list=neighbor_list, **shapes)
 
     def upload(self) -> None:
         cat = lambda k: np.concatenate([getattr(w, k) for w in self.workloads])  # noqa: E731
@@ -66,12 +68,29 @@ class BatchedSystems:
     def energies(self) -> np.ndarray:
         return self.engine.energy(per_system=True)
 
+    def tune_key(self) -> str:
+        return tune_key(self.workloads)
+
     @property
     def particles(self) -> int:
         return int(self.offsets[-1])
 
     def close(self) -> None:
         self.engine.close()
+
+
+def tune_key(workloads: Sequence[Workload]) -> str:
+    """Autotuner cache key of a batch: dimension, total particles, overall packing
+    fraction and speed (``autotune.config_key``) plus the number of systems."""
+    from .workloads import volume
+
+    dim = workloads[0].dim
+    n = sum(int(w.N) for w in workloads)
+    vol = sum(float(np.prod(np.asarray(w.box_size, np.float64))) for w in workloads)
+    occ = sum(float(volume(w.rad, w.dim).astype(np.float64).sum()) for w in workloads)
+    v2 = sum(float((np.asarray(w.vel, np.float64) ** 2).sum()) for w in workloads)
+    vrms = float(np.sqrt(v2 / max(1, n * dim)))
+    return f"batch{len(workloads)}-" + autotune.config_key(dim, n, occ / max(vol, 1e-30), vrms, "periodic")
 
 
 def step_many(states, systems, n: int):

@@ -51,3 +51,12 @@ def test_small_systems_tune_the_skin_and_lanes_per_slot(monkeypatch, tmp_path):
     assert best["skin"] == min(autotune.CANDIDATES) * 0.5 and timings["prune"] == {} and timings["block"] == {}
     assert best["small_lanes"] == 16 and best["force_block"] == 128
     assert all(p["skin"] == best["skin"] for p in seen[-len(autotune.LANE_CANDIDATES):])
+
+
+def test_batch_tune_key_separates_batches():
+    from jaxdem_gb300 import workloads as W
+    from jaxdem_gb300.batch import tune_key
+
+    a, b = W.c4(n_systems=16, seed=4), W.c4(n_systems=32, seed=4)
+    assert tune_key(a) == tune_key(W.c4(n_systems=16, seed=4))
+    assert tune_key(a) != tune_key(b) and tune_key(a).startswith("batch16-3d-periodic-")
