@@ -383,15 +383,17 @@ def run_ours(args, rank, world, dist):
 
     value = replicas.aggregate_throughput([w.N * K] * world, total_ms * 1e-3)
     # per step call of c steps: k_pre + k_fin, then the graph of c - 1 steps and the graph of
-    # the final step; per re-sort: 8 sort kernels + the list build.  Per-step graphs: k_cond
-    # each, k_force + k_fin per step.  Many-step graphs (small systems): k_multi_init, then
-    # per while iteration (one to start, one after each re-sort) 8 sort kernels, the list
-    # build and k_multi.
+    # the final step; per re-sort: the sort kernels (6, or 8 above 65,536 cells) + the list
+    # build.  Per-step graphs: k_cond each, k_force + k_fin per step.  Many-step graphs (small
+    # systems): k_multi_init, then per while iteration (one to start, one after each re-sort)
+    # the sort kernels, the list build and k_multi.
     rebuilds_timed = stats["rebuilds"] - rebuilds_before
+    # the cell scan is one kernel up to 65,536 cells, else three
+    sort_k = 6 if stats["n_cells"] <= 65536 else 8
     if stats.get("many_step"):
-        launches = sum(2 + 1 + 10 + 3 for c in chunks) + 10 * rebuilds_timed
+        launches = sum(2 + 1 + (sort_k + 2) + 3 for c in chunks) + (sort_k + 2) * rebuilds_timed
     else:
-        launches = sum(2 + 1 + 2 * (c - 1) + 3 for c in chunks) + 9 * rebuilds_timed
+        launches = sum(2 + 1 + 2 * (c - 1) + 3 for c in chunks) + (sort_k + 1) * rebuilds_timed
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,

@@ -297,6 +297,31 @@ __global__ void k_scan_down(Bufs b) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) b.cell_start[b.C] = (int)b.P;
 }
 
+// The whole exclusive scan in one block of 1024 threads for small cell counts
+// (C <= kScanSmallC): each thread sums a contiguous run of counts, the block
+// scans the run sums, and each thread writes its run's offsets.  Integer sums,
+// so the result equals the three-kernel scan's; one launch instead of three,
+// which matters when a re-sort costs launch latency rather than bandwidth.
+constexpr long long kScanSmallC = 65536;
+
+__global__ void __launch_bounds__(1024) k_scan_small(Bufs b) {
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ int sh[32];
+  const int C = (int)b.C;
+  const int per = (C + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int lo = min(C, (int)threadIdx.x * per), hi = min(C, lo + per);
+  int s = 0;
+  for (int c = lo; c < hi; ++c) s += b.cnt[c];
+  int total;
+  int off = block_excl_scan(s, sh, total);
+  for (int c = lo; c < hi; ++c) {
+    const int v = b.cnt[c];
+    b.cell_start[c] = off;
+    off += v;
+  }
+  if (threadIdx.x == 0) b.cell_start[C] = (int)b.P;
+}
+
 __global__ void k_scatter(Bufs b) {
   if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -925,6 +950,10 @@ void launch_bbox_reset(const Bufs& b, cudaStream_t st) {
 }
 
 void launch_scan(const Bufs& b, cudaStream_t st) {
+  if (b.C <= kScanSmallC) {
+    k_scan_small<<<1, 1024, 0, st>>>(b);
+    return;
+  }
   unsigned int nb = nblk(b.C, SCAN_TILE);
   k_scan_reduce<<<nb, SCAN_T, 0, st>>>(b);
   k_scan_top<<<1, 1024, 0, st>>>(b, (int)nb);
