@@ -143,3 +143,29 @@ def test_hertz_through_the_public_api():
     ok = j >= 0
     fr = R.hertz_pair(i[ok], j[ok], st2.pos_c, st2.rad, st2.mat_id, K43[:1, :1], osy)
     assert np.allclose(f[ok], fr, rtol=1e-5, atol=1e-5 * np.abs(fr).max())
+
+
+def test_hertz_large_system_with_pruning_matches_oracle_and_full_list():
+    """Above 32768 slots the fused list kernel runs the Hertz law with dynamic pruning and
+    the branch-free list batches: step-0 forces against the oracle, and 60 steps with
+    pruning equal to 60 steps on the full list bit for bit."""
+    w = periodic(N=65536, seed=45)
+    ost = ostate(w)
+    st1, _ = R.step(ost, hertz_sys(w), 1, sum_dtype=np.float64)
+    outs = []
+    for ps in (0.0, -1.0):
+        eng = Engine(w.dim, [w.desc()], K43[:1, :1], skin=0.3, force_law="hertz", prune_skin=ps)
+        try:
+            eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+            eng.step(1)
+            first = eng.download()
+            eng.step(59)
+            outs.append((first, eng.download(), eng.stats()))
+        finally:
+            eng.close()
+    (f_pr, pr, st_pr), (f_full, full, st_full) = outs
+    assert force_err(f_pr["force"], st1.force) <= 1e-5
+    assert min_image_diff(f_pr["pos_c"], st1.pos_c, w.box_size) <= 1e-5
+    assert st_pr["prunes"] > 0 and st_full["prunes"] == 0
+    for k in ("pos_c", "vel", "force"):
+        assert np.array_equal(pr[k], full[k]), k
