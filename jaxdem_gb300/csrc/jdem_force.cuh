@@ -67,9 +67,25 @@ __global__ void __launch_bounds__(128) k_force_small(Bufs b, int mode) {
     if (use_list) {
       const int n = b.ncnt[t];
       const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
-      for (int k = g; k < n; k += G) {
-        const uint32_t e = (uint32_t)nb[k * 32];
-        acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], GENERAL || (e & kEntryImage) != 0u);
+      if (GENERAL) {
+        for (int k = g; k < n; k += G) {
+          const uint32_t e = (uint32_t)nb[k * 32];
+          acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], GENERAL || (e & kEntryImage) != 0u);
+        }
+      } else {
+        // the lane's entries g, g + G, ... four at a time, without branches (padding
+        // entries take the slot's own position and add nothing): the same terms in
+        // the same order as one entry at a time
+        for (int k0 = g; k0 < n; k0 += 4 * G) {
+          uint32_t e[4];
+          float4 q[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) e[u] = k0 + u * G < n ? (uint32_t)nb[(k0 + u * G) * 32] : 0u;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) q[u] = P[k0 + u * G < n ? (long long)(e[u] & kEntrySlot) : t];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, k0 + u * G < n);
+        }
       }
     } else {
       int c = 0;

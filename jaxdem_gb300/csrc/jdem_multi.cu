@@ -161,9 +161,16 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
 #pragma unroll
         for (int i = 0; i < kMultiE; ++i) q[i] = g + i * G < n ? ldc4(&P[ent[i] & kEntrySlot]) : pi;
 #pragma unroll
-        for (int i = 0; i < kMultiE; ++i)
-          if (g + i * G < n)
-            acc.add(b, sel, (int)(ent[i] & kEntrySlot), q[i], GENERAL || (ent[i] & kEntryImage) != 0u);
+        for (int i = 0; i < kMultiE; ++i) {
+          if (GENERAL) {
+            if (g + i * G < n)
+              acc.add(b, sel, (int)(ent[i] & kEntrySlot), q[i], GENERAL || (ent[i] & kEntryImage) != 0u);
+          } else {
+            // branch-free (the padding entries hold the slot's own position): the
+            // entries' arithmetic interleaves, and the sums equal k_force_small's
+            acc.add_plain(q[i], (ent[i] & kEntryImage) != 0u, g + i * G < n);
+          }
+        }
         for (int k = g + kMultiE * G; k < n; k += G) {
           const uint32_t e = (uint32_t)nb[k * 32];
           acc.add(b, sel, (int)(e & kEntrySlot), ldc4(&P[e & kEntrySlot]), GENERAL || (e & kEntryImage) != 0u);
