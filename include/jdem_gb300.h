@@ -156,7 +156,9 @@ typedef struct {
   int32_t dim;
   int64_t rebuilds;          /* re-sorts since the last upload */
   int64_t steps;             /* steps since the last upload */
-  uint32_t device_status;    /* sticky device status bits */
+  uint32_t device_status;    /* sticky device status bits: 1 non-finite state, 2 capacity,
+                                4 neighbour overflow, 16 grid-barrier timeout, 32 an index
+                                out of range (only the bounds-checked build sets it) */
   int32_t graphs;            /* instantiated CUDA graphs */
   int64_t device_bytes;      /* device memory held by the handle */
   int64_t list_regrowths;    /* Verlet-list capacity doublings after a row overflowed */

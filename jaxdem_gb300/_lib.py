@@ -14,7 +14,9 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libjdem_gb300.so"
+# JDEM_LIBRARY names another build of the same library: the bounds-checked one
+# (build.build(checked=True)) in the tests that run it
+LIB_PATH = Path(os.environ.get("JDEM_LIBRARY") or Path(__file__).resolve().parent / "_lib" / "libjdem_gb300.so")
 
 JDEM_OK = 0
 STATUS_NAMES = {

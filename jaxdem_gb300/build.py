@@ -26,6 +26,9 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libjdem_gb300.so"
+# the bounds-checked build (-DJDEM_BOUNDS_CHECK: every range check of the kernels
+# compiled in, a failed one reported as a device status bit); for tests only
+CHECKED_LIB = OUT_DIR / "libjdem_gb300_checked.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # translation units free of reference arithmetic: multiply-add contraction allowed
@@ -43,28 +46,31 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
-def _stale() -> bool:
-    if not LIB.exists():
+def _stale(lib: Path = LIB) -> bool:
+    if not lib.exists():
         return True
-    t = LIB.stat().st_mtime
+    t = lib.stat().st_mtime
     deps = list(CSRC.glob("*")) + list((PKG.parent / "include").glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile the CUDA sources and link the shared library; returns its path."""
-    if not force and not _stale():
-        return LIB
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile the CUDA sources and link the shared library; returns its path.
+    ``checked`` builds the bounds-checked library (``CHECKED_LIB``) instead."""
+    lib = CHECKED_LIB if checked else LIB
+    if not force and not _stale(lib):
+        return lib
     OUT_DIR.mkdir(exist_ok=True)
-    obj_dir = OUT_DIR / "obj"
+    obj_dir = OUT_DIR / ("obj_checked" if checked else "obj")
     obj_dir.mkdir(exist_ok=True)
     cc = nvcc()
     inc = ["-I", str(PKG.parent / "include"), "-I", str(CSRC)]
+    defs = ["-DJDEM_BOUNDS_CHECK"] if checked else []
 
     def compile_one(src: Path) -> Path:
         obj = obj_dir / (src.stem + ".o")
         fmad = [] if src.name in CONTRACT_OK else ["-fmad=false"]
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *inc, "-c", str(src), "-o", str(obj)]
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *defs, *inc, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -75,16 +81,17 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
     if verbose:
         print(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    build_xla_ffi(LIB)
-    return LIB
+    os.replace(tmp, lib)
+    if not checked:
+        build_xla_ffi(LIB)
+    return lib
 
 
 def jax_ffi_include() -> Path | None:

@@ -65,11 +65,13 @@ __global__ void __launch_bounds__(128) k_force_small(Bufs b, int mode) {
     const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
     ContactSum<DIM, GENERAL, LAW> acc(b, sp, pi, tg, sel, t);
     if (use_list) {
-      const int n = b.ncnt[t];
+      int n = b.ncnt[t];
+      if (!idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
       const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
       if (GENERAL) {
         for (int k = g; k < n; k += G) {
-          const uint32_t e = (uint32_t)nb[k * 32];
+          uint32_t e = (uint32_t)nb[k * 32];
+          if (!idx_ok(b.ctl, e & kEntrySlot, b.P)) e = (uint32_t)t;
           acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], GENERAL || (e & kEntryImage) != 0u);
         }
       } else {
@@ -82,7 +84,8 @@ __global__ void __launch_bounds__(128) k_force_small(Bufs b, int mode) {
 #pragma unroll
           for (int u = 0; u < 4; ++u) e[u] = k0 + u * G < n ? (uint32_t)nb[(k0 + u * G) * 32] : 0u;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) q[u] = P[k0 + u * G < n ? (long long)(e[u] & kEntrySlot) : t];
+          for (int u = 0; u < 4; ++u)
+            q[u] = P[k0 + u * G < n && idx_ok(b.ctl, e[u] & kEntrySlot, b.P) ? (long long)(e[u] & kEntrySlot) : t];
 #pragma unroll
           for (int u = 0; u < 4; ++u) acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, k0 + u * G < n);
         }

@@ -199,6 +199,7 @@ __global__ void k_bin(Bufs b) {
     local += (long long)cz * sp.g[0] * sp.g[1];
   }
   int key = (int)(sp.c0 + local);
+  if (!idx_ok(b.ctl, key, b.C)) key = 0;
   b.key_tmp[t] = key;
   // one atomic per distinct cell of the warp: slots are ordered by cell since
   // the last re-sort, so neighbouring lanes mostly share a cell
@@ -327,7 +328,9 @@ __global__ void k_scatter(Bufs b) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= b.P) return;
   int key = b.key_tmp[t];
-  b.perm_tmp[b.cell_start[key] + b.slot_tmp[t]] = (int)t;
+  if (!idx_ok(b.ctl, key, b.C)) return;
+  const long long dst = (long long)b.cell_start[key] + b.slot_tmp[t];
+  if (idx_ok(b.ctl, dst, b.P)) b.perm_tmp[dst] = (int)t;
 }
 
 // Per cell: order the cell's slots by original index (the stable order of
@@ -340,6 +343,9 @@ __global__ void k_cellsort(Bufs b) {
   int a = b.cell_start[c], e = b.cell_start[c + 1];
   b.cnt[c] = 0;
   const int32_t* orig = b.orig[sel];
+  if (!idx_ok(b.ctl, a, b.P + 1) || !idx_ok(b.ctl, e, b.P + 1)) return;
+  for (int i = a; i < e; ++i)
+    if (!idx_ok(b.ctl, b.perm_tmp[i], b.P)) return;
   for (int i = a + 1; i < e; ++i) {
     int x = b.perm_tmp[i];
     int ox = orig[x];
@@ -360,6 +366,7 @@ __global__ void k_gather(Bufs b) {
   unsigned int sel = ld_nc_u32(&b.ctl->sel), ps = ld_nc_u32(&b.ctl->pos_sel);
   if (u < b.P) {
     int t = __ldcs(&b.perm_tmp[u]);  // old-order records are read once: streaming loads
+    if (!idx_ok(b.ctl, t, b.P)) t = (int)u;
     const float4 p = __ldcs(&b.pos[ps][t]);
     b.pos[ps ^ 1u][u] = p;
     if (b.posw) {

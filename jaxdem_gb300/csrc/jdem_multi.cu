@@ -137,11 +137,13 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
     if (g == 0) v4 = ldc4(&b.vel[sel][t]);
     if (use_list) {
       n = b.ncnt[t];
+      if (!idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
       nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
 #pragma unroll
       for (int i = 0; i < kMultiE; ++i) {
         const int k = g + i * G;
         ent[i] = k < n ? (uint32_t)nb[k * 32] : 0u;
+        if (k < n && !idx_ok(b.ctl, ent[i] & kEntrySlot, b.P)) ent[i] = (uint32_t)t;
       }
     }
   }
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(kMultiT) k_multi(Bufs b, cudaGraphConditionalH
           }
         }
         for (int k = g + kMultiE * G; k < n; k += G) {
-          const uint32_t e = (uint32_t)nb[k * 32];
+          uint32_t e = (uint32_t)nb[k * 32];
+          if (!idx_ok(b.ctl, e & kEntrySlot, b.P)) e = (uint32_t)t;
           acc.add(b, sel, (int)(e & kEntrySlot), ldc4(&P[e & kEntrySlot]), GENERAL || (e & kEntryImage) != 0u);
         }
       } else {

@@ -305,6 +305,7 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
   const uint32_t tg = b.tag[sel][t];
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
   ContactSum<DIM, GENERAL, LAW> acc(b, sp, pi, tg, sel, t);
+  if (use_list && !idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
   // Rows without GENERAL lookups load four words and four positions per batch
   // without per-entry branches: list rows hold a multiple of four entries, so
   // the last batch's words stay inside the row, and its padding entries load
@@ -317,13 +318,14 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
 #pragma unroll
       for (int u = 0; u < 4; ++u) e[u] = (uint32_t)__ldcs(&nb[(k + u) * stride]);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) q[u] = P[k + u < n ? (long long)(e[u] & kEntrySlot) : t];
+      for (int u = 0; u < 4; ++u)
+        q[u] = P[k + u < n && idx_ok(b.ctl, e[u] & kEntrySlot, b.P) ? (long long)(e[u] & kEntrySlot) : t];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const bool valid = k + u < n;
         const float dsq = acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, valid);
         const float rc = (pi.w + q[u].w + b.prune_skin) * 1.0001f;
-        if (valid && dsq < rc * rc) prune_out[(m++) * stride] = (int32_t)e[u];
+        if (valid && dsq < rc * rc && idx_ok(b.ctl, m, b.nl_cap)) prune_out[(m++) * stride] = (int32_t)e[u];
       }
     }
     *prune_cnt = m;
@@ -336,7 +338,8 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
 #pragma unroll
       for (int u = 0; u < 4; ++u) e[u] = (uint32_t)__ldcs(&nb[(k + u) * stride]);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) q[u] = P[k + u < n ? (long long)(e[u] & kEntrySlot) : t];
+      for (int u = 0; u < 4; ++u)
+        q[u] = P[k + u < n && idx_ok(b.ctl, e[u] & kEntrySlot, b.P) ? (long long)(e[u] & kEntrySlot) : t];
 #pragma unroll
       for (int u = 0; u < 4; ++u) acc.add_plain(q[u], (e[u] & kEntryImage) != 0u, k + u < n);
     }
@@ -349,13 +352,16 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
 #pragma unroll
       for (int u = 0; u < 4; ++u) e[u] = k + u < n ? (uint32_t)__ldcs(&nb[(k + u) * stride]) : 0u;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
+      for (int u = 0; u < 4; ++u) {
+        if (k + u < n && !idx_ok(b.ctl, e[u] & kEntrySlot, b.P)) e[u] = (uint32_t)t;
+        q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
+      }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (k + u < n) {
           const float dsq = acc.add(b, sel, (int)(e[u] & kEntrySlot), q[u], GENERAL || (e[u] & kEntryImage) != 0u);
           const float rc = (pi.w + q[u].w + b.prune_skin) * 1.0001f;
-          if (dsq < rc * rc) prune_out[(m++) * stride] = (int32_t)e[u];
+          if (dsq < rc * rc && idx_ok(b.ctl, m, b.nl_cap)) prune_out[(m++) * stride] = (int32_t)e[u];
         }
       }
     }
@@ -367,16 +373,21 @@ __device__ __forceinline__ float particle_step(const Bufs& b, int mode, long lon
 #pragma unroll
       for (int u = 0; u < 4; ++u) e[u] = k + u < n ? (uint32_t)__ldcs(&nb[(k + u) * stride]) : 0u;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
+      for (int u = 0; u < 4; ++u) {
+        if (k + u < n && !idx_ok(b.ctl, e[u] & kEntrySlot, b.P)) e[u] = (uint32_t)t;
+        q[u] = k + u < n ? P[e[u] & kEntrySlot] : pi;
+      }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (k + u < n) acc.add(b, sel, (int)(e[u] & kEntrySlot), q[u], GENERAL || (e[u] & kEntryImage) != 0u);
       }
     }
   } else {
-    for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) {
-      if (j != (int)t) acc.add(b, sel, j, P[j]);
-    });
+    const long long local = b.key[sel][t] - sp.c0;
+    if (idx_ok(b.ctl, local, (long long)sp.g[0] * sp.g[1] * (DIM == 3 ? sp.g[2] : 1)))
+      for_each_candidate<DIM>(b.cell_start, sp, local, [&](int j) {
+        if (j != (int)t) acc.add(b, sel, j, P[j]);
+      });
   }
   float F[3] = {acc.fx + acc.ex, acc.fy + acc.ey, DIM == 3 ? acc.fz + acc.ez : 0.0f};
   // loaded after the contact loop: holding it through the loop costs registers

@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
   const int32_t* __restrict__ cs = b.cell_start;
   const unsigned int sel = ld_nc_u32(&b.ctl->sel);
   bool direct = (td.flags & TILE_DIRECT) != 0 || NV > NVC || nrows > NR;
+  if (!idx_ok(b.ctl, HD, kMaxHomeRows + 1)) return;  // block-uniform
 
   if (!direct) {
     // occupancy of every virtual cell -> staged offsets
@@ -225,6 +226,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
       const int y = td.y0 + r % bk.H, z = DIM == 3 ? td.z0 + r / bk.H : 0;
       const long long row = sp.c0 + ((long long)z * sp.g[1] + y) * sp.g[0];
       const long long slot = cs[row + td.x0] + (h - s_hrow[r]);
+      if (!idx_ok(b.ctl, slot, b.P)) continue;
       const float4 pi = Pc[slot];
       int32_t* out = b.nbr + ((slot >> 5) * cap) * 32 + (slot & 31);
       int n = 0;
@@ -262,6 +264,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
         const int ja = splan[6 * r + k], len = splan[6 * r + 3 + k];
         const int32_t shifted = (row_shifted || k != 1) ? (int32_t)0x80000000 : 0;
         for (int i = lane; i < len; i += 32) {
+          if (!idx_ok(b.ctl, o + i, NST) || !idx_ok(b.ctl, ja + i, b.P)) continue;
           float4 w = b.posw[ja + i];
           w.x = w.x + sx[k];
           w.y = w.y + syz[0];
@@ -290,6 +293,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
     const int rb = (iz * bk.VY + iy) * bk.VX;
     const int oh = vstart[rb + 1] + (h - s_hrow[r]);
     const int ix = last_le(vstart, rb + 1, rb + bk.W + 1, oh) - rb;  // virtual x of the home cell
+    if (!idx_ok(b.ctl, oh, vstart[NV])) continue;
     const long long slot = sslot[oh];
     const float4 pi = spos[oh];
     // (r_i + r_j + skin) * 1.0001 + eps with the staged radii already widened
@@ -304,6 +308,7 @@ __global__ void __launch_bounds__(TB) k_tbuild(Bufs b) {
 #pragma unroll 1
       for (int dy = -1; dy <= 1; ++dy) {
         const int vb = ((iz + dz) * bk.VY + (iy + dy)) * bk.VX + ix - 1;
+        if (!idx_ok(b.ctl, vb, NV - 2)) continue;
         const int oa = vstart[vb], ob = vstart[vb + 3];
         auto test = [&](int oj, const float4& q) {
           const float ddx = pi.x - q.x, ddy = pi.y - q.y;

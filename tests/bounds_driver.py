@@ -1,0 +1,97 @@
+"""Child process of ``test_gpu_bounds.py``: the engine's main paths at small sizes.
+
+Loads whichever engine library ``JDEM_LIBRARY`` names (the regular or the bounds-checked
+build) and prints one JSON line per case: the sticky device status after the case, the
+number of contacts, and a digest of the final positions, velocities and forces.  Cases:
+the many-step kernel (4096 spheres), the fused list kernel with the brick list build and
+pruning (40,000 spheres, both block shapes, 2D and 3D), two materials with the Hertz law
+(the general contact path, pruned), a reflecting 2D box with gravity, a free domain (the
+per-slot list build), 3,000 spheres at 16 lanes a slot, a batch of twelve uneven systems,
+the neighbour-list API and a streamed rollout.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+from jaxdem_gb300 import workloads as W  # noqa: E402
+from jaxdem_gb300._lib import Engine  # noqa: E402
+from jaxdem_gb300.forces import hertz_pair_constant  # noqa: E402
+
+K = np.array([[W.K_SPRING]], np.float32)
+
+
+def digest(out: dict) -> str:
+    h = hashlib.sha1()
+    for k in ("pos_c", "vel", "force"):
+        h.update(np.ascontiguousarray(out[k]).tobytes())
+    return h.hexdigest()[:16]
+
+
+def report(tag: str, eng: Engine, extra: dict | None = None) -> None:
+    out = eng.download()
+    rec = {"case": tag, "status": int(eng.stats()["device_status"]), "contacts": int(len(eng.contacts())),
+           "digest": digest(out)}
+    rec.update(extra or {})
+    print(json.dumps(rec), flush=True)
+
+
+def run(tag, w, steps=30, young=K, mat_id=None, **kw):
+    eng = Engine(w.dim, [w.desc()], young, **kw)
+    try:
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat_id)
+        eng.compute_force()
+        eng.step(steps)
+        report(tag, eng, {"rebuilds": int(eng.stats()["rebuilds"])})
+    finally:
+        eng.close()
+
+
+def main() -> None:
+    run("many_step_4096", W.c1())
+    run("list_pruned_40000", W.c2(N=40000), skin=0.63, prune_skin=0.315)
+    run("list_block64_40000", W.c2(N=40000), skin=0.3, prune_skin=-1.0, force_block=64)
+    w = W.c2(N=40000)
+    mats = np.random.default_rng(3).integers(0, 2, size=40000).astype(np.int32)
+    run("hertz_two_materials_40000", w, young=hertz_pair_constant([1e3, 2e3], [0.3, 0.25]), mat_id=mats,
+        skin=0.4, force_law="hertz")
+    w2 = W.periodic_system("p2", np.random.Generator(np.random.PCG64(5)), 40000, 2,
+                           np.where(np.arange(40000) % 2 == 0, 0.5, 0.7), 0.7, 0.05, 5e-4, 30)
+    run("list_2d_40000", w2, skin=0.5, force_block=256)
+    run("reflect_2d_40000", W.c3(N=40000), skin=0.2)
+    w = W.c2(N=40000)
+    w.domain = "free"
+    run("free_40000", w, skin=0.3)
+    run("small_lanes16_3000", W.c2(N=3000), skin=0.3, small_lanes=16)
+    ws = W.c4(n_systems=12, n_max=3000)
+    eng = Engine(3, [x.desc() for x in ws], K, skin=0.2)
+    try:
+        cat = lambda k: np.concatenate([getattr(x, k) for x in ws])  # noqa: E731
+        eng.upload(pos=cat("pos"), rad=cat("rad"), mass=cat("mass"), vel=cat("vel"))
+        eng.step(30)
+        report("batch_12_systems", eng)
+    finally:
+        eng.close()
+    w = W.c1()
+    eng = Engine(3, [w.desc()], K)
+    try:
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel)
+        nl, overflow = eng.neighbor_list(1.2, 32)
+        frames = eng.rollout([1, 2, 3, 4])
+        h = hashlib.sha1(np.ascontiguousarray(nl).tobytes() + np.ascontiguousarray(frames["pos_c"]).tobytes())
+        report("neighbor_list_rollout_4096", eng, {"nlist": h.hexdigest()[:16], "overflow": bool(overflow)})
+    finally:
+        eng.close()
+
+
+if __name__ == "__main__":
+    main()
