@@ -45,11 +45,13 @@ __global__ void k_cs_force(Bufs b) {
   const bool per = sp.domain == DOM_PERIODIC;
   const int mi = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
   const int oi = b.orig[sel][t];
+  if (!idx_ok(b.ctl, oi, b.P)) return;
   const float vi[3] = {vi4.x, vi4.y, vi4.z};
   float wi[3] = {0.0f, 0.0f, 0.0f};
   for (int a = 0; a < AD; ++a) wi[a] = b.rw[(long long)oi * AD + a];
   float F[3] = {0, 0, 0}, eF[3] = {0, 0, 0}, T[3] = {0, 0, 0}, eT[3] = {0, 0, 0};
   auto visit = [&](int j, bool may_wrap) {
+    if (!idx_ok(b.ctl, j, b.P)) return;
     const float4 pj = P[j];
     float d[3];
     const float dsq = pair_disp<DIM>(sp, per && may_wrap, pi, pj, d[0], d[1], d[2]);
@@ -69,7 +71,8 @@ __global__ void k_cs_force(Bufs b) {
     cs_pair<DIM>(b, mi, mj, pi.w, pj.w, vi4.w, vj4.w, vi, vj, wi, wj, d, F, eF, T, eT);
   };
   if (use_list) {
-    const int n = b.ncnt[t];
+    int n = b.ncnt[t];
+    if (!idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
     const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
     prefetch_list_block(b, t, n);
     for (int k = 0; k < n; ++k) {
@@ -77,9 +80,11 @@ __global__ void k_cs_force(Bufs b) {
       visit((int)(e & kEntrySlot), (e & kEntryImage) != 0u);
     }
   } else {
-    for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) {
-      if (j != (int)t) visit(j, true);
-    });
+    const long long local = b.key[sel][t] - sp.c0;
+    if (idx_ok(b.ctl, local, (long long)sp.g[0] * sp.g[1] * (DIM == 3 ? sp.g[2] : 1)))
+      for_each_candidate<DIM>(b.cell_start, sp, local, [&](int j) {
+        if (j != (int)t) visit(j, true);
+      });
   }
   b.frc[sel][t] = make_float4(F[0] + eF[0], F[1] + eF[1], DIM == 3 ? F[2] + eF[2] : 0.0f, 0.0f);
   // compute_force's epilogue adds cross(pos_p, F) = 0 for spheres (cell_list.py:452-464)

@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
   const uint32_t mark = per ? kEntryImage : 0u;
   int n = 0;
   auto range = [&](int ja, int jb, float sx, float sy, float sz) {
+    if (!idx_ok(b.ctl, ja, b.P + 1) || !idx_ok(b.ctl, jb, b.P + 1)) return;
     for (int j = ja; j < jb; j += 4) {
       float4 q[4];
 #pragma unroll
@@ -534,6 +535,7 @@ __global__ void __launch_bounds__(256) k_nlbuild(Bufs b) {
     int ny = axis_set(cy, gy, per, ys);
     int nz = DIM == 3 ? axis_set(cz, gz, per, zs) : 1;
     if (DIM == 2) zs[0] = 0;
+    if (!idx_ok(b.ctl, local, (long long)gx * gy * (DIM == 3 ? gz : 1))) nz = 0;
     int xa0, xb0, xa1, xb1;
     x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
     // image shifts (only used when `shifted`)
@@ -635,6 +637,8 @@ __global__ void k_energy(Bufs b, double* __restrict__ out) {
   x_ranges(cx, gx, per, xa0, xb0, xa1, xb1);
   const int mat_i = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
   const int oi = b.orig[sel][t];
+  if (!idx_ok(b.ctl, oi, b.P)) return;
+  if (!idx_ok(b.ctl, local, (long long)gx * gy * (DIM == 3 ? sp.g[2] : 1))) nz = 0;
   for (int iz = 0; iz < nz; ++iz)
     for (int iy = 0; iy < ny; ++iy) {
       long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;
@@ -747,6 +751,7 @@ __global__ void k_contacts(Bufs b, int pass, int32_t* __restrict__ counts,
   int oi = b.orig[sel][t];
   long long o = pass == 1 ? offs[t] : 0;
   int c = 0;
+  if (!idx_ok(b.ctl, local, (long long)gx * gy * (DIM == 3 ? sp.g[2] : 1))) nz = 0;
   for (int iz = 0; iz < nz; ++iz)
     for (int iy = 0; iy < ny; ++iy) {
       long long row = sp.c0 + ((long long)zs[iz] * gy + ys[iy]) * gx;

@@ -5,9 +5,10 @@ build) and prints one JSON line per case: the sticky device status after the cas
 number of contacts, and a digest of the final positions, velocities and forces.  Cases:
 the many-step kernel (4096 spheres), the fused list kernel with the brick list build and
 pruning (40,000 spheres, both block shapes, 2D and 3D), two materials with the Hertz law
-(the general contact path, pruned), a reflecting 2D box with gravity, a free domain (the
-per-slot list build), 3,000 spheres at 16 lanes a slot, a batch of twelve uneven systems,
-the neighbour-list API and a streamed rollout.
+(the general contact path, pruned), Cundall-Strack with spin and two materials, a
+reflecting 2D box with gravity, a free domain (the per-slot list build), 3,000 spheres at
+16 lanes a slot, a batch of twelve uneven systems, the neighbour-list API and a streamed
+rollout.
 """
 
 from __future__ import annotations
@@ -25,7 +26,7 @@ import numpy as np  # noqa: E402
 
 from jaxdem_gb300 import workloads as W  # noqa: E402
 from jaxdem_gb300._lib import Engine  # noqa: E402
-from jaxdem_gb300.forces import hertz_pair_constant  # noqa: E402
+from jaxdem_gb300.forces import cundall_strack_tables, hertz_pair_constant  # noqa: E402
 
 K = np.array([[W.K_SPRING]], np.float32)
 
@@ -45,10 +46,12 @@ def report(tag: str, eng: Engine, extra: dict | None = None) -> None:
     print(json.dumps(rec), flush=True)
 
 
-def run(tag, w, steps=30, young=K, mat_id=None, **kw):
-    eng = Engine(w.dim, [w.desc()], young, **kw)
+def run(tag, w, steps=30, young=K, mat_id=None, ang_vel=None, rotation="", **kw):
+    d = w.desc()
+    d["rotation"] = rotation
+    eng = Engine(w.dim, [d], young, **kw)
     try:
-        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat_id)
+        eng.upload(pos=w.pos, rad=w.rad, mass=w.mass, vel=w.vel, mat_id=mat_id, ang_vel=ang_vel)
         eng.compute_force()
         eng.step(steps)
         report(tag, eng, {"rebuilds": int(eng.stats()["rebuilds"])})
@@ -64,6 +67,11 @@ def main() -> None:
     mats = np.random.default_rng(3).integers(0, 2, size=40000).astype(np.int32)
     run("hertz_two_materials_40000", w, young=hertz_pair_constant([1e3, 2e3], [0.3, 0.25]), mat_id=mats,
         skin=0.4, force_law="hertz")
+    beta, props = cundall_strack_tables([1e3, 3e3], [0.25, 0.3], [0.6, 0.8], [0.4, 0.3], [0.05, 0.1])
+    w = W.c2(N=40000)
+    spin = np.random.default_rng(4).normal(0.0, 2.0, size=(40000, 3)).astype(np.float32)
+    run("cundall_strack_40000", w, young=beta, mat_id=mats, ang_vel=spin, rotation="verletspiral", skin=0.3,
+        force_law="cundallstrack", material_props=props)
     w2 = W.periodic_system("p2", np.random.Generator(np.random.PCG64(5)), 40000, 2,
                            np.where(np.arange(40000) % 2 == 0, 0.5, 0.7), 0.7, 0.05, 5e-4, 30)
     run("list_2d_40000", w2, skin=0.5, force_block=256)
