@@ -54,20 +54,24 @@ __global__ void k_rb_force(Bufs b) {
   const SysParams& sp = b.sys[tg & TAG_SYS_MASK];
   ContactSum<DIM, true, LAW> acc(b, sp, pi, tg, sel, t);
   if (use_list) {
-    const int n = b.ncnt[t];
+    int n = b.ncnt[t];
+    if (!idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
     const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
     prefetch_list_block(b, t, n);
     for (int k = 0; k < n; ++k) {
       const uint32_t e = (uint32_t)nb[k * 32];
-      acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], true);
+      if (idx_ok(b.ctl, e & kEntrySlot, b.P)) acc.add(b, sel, (int)(e & kEntrySlot), P[e & kEntrySlot], true);
     }
   } else {
-    for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) {
-      if (j != (int)t) acc.add(b, sel, j, P[j]);
-    });
+    const long long local = b.key[sel][t] - sp.c0;
+    if (idx_ok(b.ctl, local, (long long)sp.g[0] * sp.g[1] * (DIM == 3 ? sp.g[2] : 1)))
+      for_each_candidate<DIM>(b.cell_start, sp, local, [&](int j) {
+        if (j != (int)t) acc.add(b, sel, j, P[j]);
+      });
   }
   const float F[3] = {acc.fx + acc.ex, acc.fy + acc.ey, DIM == 3 ? acc.fz + acc.ez : 0.0f};
   const long long i = b.orig[sel][t];
+  if (!idx_ok(b.ctl, i, b.P) || !idx_ok(b.ctl, b.sclump[i], b.NC)) return;
   float r[3] = {0.0f, 0.0f, 0.0f};
   lever<DIM>(b, b.cq[b.sclump[i]], i, r);
   // torque = sum of pair torques (0 for these laws) + cross(R(q) pos_p, F)
@@ -102,18 +106,21 @@ __global__ void k_rb_cs_force(Bufs b) {
   const bool per = sp.domain == DOM_PERIODIC;
   const int mi = (tg >> TAG_MAT_SHIFT) & TAG_MAT_MASK;
   const long long oi = b.orig[sel][t];
+  if (!idx_ok(b.ctl, oi, b.P) || !idx_ok(b.ctl, b.sclump[oi], b.NC)) return;
   const int ci = b.sclump[oi];
   const float4 vi4 = b.cvel[ci], wi4 = b.cw[ci];
   const float Mi = b.cpos[ci].w;
   const float vi[3] = {vi4.x, vi4.y, vi4.z}, wi[3] = {wi4.x, wi4.y, wi4.z};
   float F[3] = {0, 0, 0}, eF[3] = {0, 0, 0}, T[3] = {0, 0, 0}, eT[3] = {0, 0, 0};
   auto visit = [&](int j, bool may_wrap) {
+    if (!idx_ok(b.ctl, j, b.P)) return;
     const float4 pj = P[j];
     float d[3];
     const float dsq = pair_disp<DIM>(sp, per && may_wrap, pi, pj, d[0], d[1], d[2]);
     const float R = pi.w + pj.w;
     if (!(dsq < R * R * 1.000001f)) return;
     const int oj = b.orig[sel][j];
+    if (!idx_ok(b.ctl, oj, b.P) || !idx_ok(b.ctl, b.sclump[oj], b.NC)) return;
     const int cj = b.sclump[oj];
     if (cj == ci) return;  // one body (valid_interaction_mask)
     if (b.bond_w > 0 && !b.interact_same_bond) {
@@ -127,7 +134,8 @@ __global__ void k_rb_cs_force(Bufs b) {
     cs_pair<DIM>(b, mi, mj, pi.w, pj.w, Mi, b.cpos[cj].w, vi, vj, wi, wj, d, F, eF, T, eT);
   };
   if (use_list) {
-    const int n = b.ncnt[t];
+    int n = b.ncnt[t];
+    if (!idx_ok(b.ctl, n, (long long)b.nl_cap + 1)) n = 0;
     const int32_t* nb = b.nbr + ((t >> 5) * b.nl_cap) * 32 + (t & 31);
     prefetch_list_block(b, t, n);
     for (int k = 0; k < n; ++k) {
@@ -135,9 +143,11 @@ __global__ void k_rb_cs_force(Bufs b) {
       visit((int)(e & kEntrySlot), (e & kEntryImage) != 0u);
     }
   } else {
-    for_each_candidate<DIM>(b.cell_start, sp, b.key[sel][t] - sp.c0, [&](int j) {
-      if (j != (int)t) visit(j, true);
-    });
+    const long long local = b.key[sel][t] - sp.c0;
+    if (idx_ok(b.ctl, local, (long long)sp.g[0] * sp.g[1] * (DIM == 3 ? sp.g[2] : 1)))
+      for_each_candidate<DIM>(b.cell_start, sp, local, [&](int j) {
+        if (j != (int)t) visit(j, true);
+      });
   }
   const float f[3] = {F[0] + eF[0], F[1] + eF[1], DIM == 3 ? F[2] + eF[2] : 0.0f};
   float r[3] = {0.0f, 0.0f, 0.0f};

@@ -7,8 +7,8 @@ the many-step kernel (4096 spheres), the fused list kernel with the brick list b
 pruning (40,000 spheres, both block shapes, 2D and 3D), two materials with the Hertz law
 (the general contact path, pruned), Cundall-Strack with spin and two materials, a
 reflecting 2D box with gravity, a free domain (the per-slot list build), 3,000 spheres at
-16 lanes a slot, a batch of twelve uneven systems, the neighbour-list API and a streamed
-rollout.
+16 lanes a slot, rigid clumps under the spring and Cundall-Strack laws, a batch of twelve
+uneven systems, the neighbour-list API and a streamed rollout.
 """
 
 from __future__ import annotations
@@ -59,6 +59,46 @@ def run(tag, w, steps=30, young=K, mat_id=None, ang_vel=None, rotation="", **kw)
         eng.close()
 
 
+def clumps(n_clumps=1500, seed=61, phi=0.35):
+    """Rigid dumbbells and triangles (and single spheres) at random centres, orientations
+    and spins in a periodic 3D box, per-member arrays in the reference layout."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([1, 2, 3], n_clumps, p=[0.2, 0.5, 0.3])
+    n = int(sizes.sum())
+    rad = rng.uniform(0.4, 0.5, n).astype(np.float32)
+    vol = 4.0 / 3.0 * np.pi * rad.astype(np.float64) ** 3
+    box = float((vol.sum() / phi) ** (1.0 / 3.0))
+    cid = np.repeat(np.arange(n_clumps), sizes)
+    offsets = {1: [[0.0, 0.0, 0.0]], 2: [[-0.35, 0.0, 0.0], [0.35, 0.0, 0.0]],
+               3: [[-0.3, -0.2, 0.0], [0.3, -0.2, 0.0], [0.0, 0.35, 0.0]]}
+    pos_p = np.concatenate([offsets[int(k)] for k in sizes]).astype(np.float32)
+    q = rng.normal(size=(n_clumps, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    mass = np.bincount(cid, weights=vol)
+    inertia = np.stack([mass * 0.2 + 0.05 * a for a in range(3)], 1)
+    arrays = dict(pos=rng.uniform(0, box, (n_clumps, 3))[cid], q=q[cid], vel=rng.normal(0, 0.3, (n_clumps, 3))[cid],
+                  ang_vel=rng.normal(0, 1.0, (n_clumps, 3))[cid], mass=mass[cid], inertia=inertia[cid])
+    arrays = {k: v.astype(np.float32) for k, v in arrays.items()}
+    desc = dict(n=n, domain="periodic", linear="verlet", rotation="verletspiral", dt=1e-3,
+                box_size=np.full(3, box, np.float32), anchor=np.zeros(3, np.float32), restitution=1.0,
+                gravity=np.zeros(3, np.float32), cell_size=1.0, search_range=1)
+    return desc, dict(rad=rad, pos_p=pos_p, clump_id=cid.astype(np.int32), **arrays)
+
+
+def run_clumps(tag, young, **kw):
+    desc, c = clumps()
+    eng = Engine(3, [desc], young, skin=0.1, **kw)
+    try:
+        eng.upload(pos=c["pos"], rad=c["rad"], mass=c["mass"], vel=c["vel"], q=c["q"], ang_vel=c["ang_vel"],
+                   inertia=c["inertia"], pos_p=c["pos_p"], clump_id=c["clump_id"],
+                   mat_id=(c["clump_id"] % 2).astype(np.int32) if kw.get("force_law") else None)
+        eng.compute_force()
+        eng.step(30)
+        report(tag, eng)
+    finally:
+        eng.close()
+
+
 def main() -> None:
     run("many_step_4096", W.c1())
     run("list_pruned_40000", W.c2(N=40000), skin=0.63, prune_skin=0.315)
@@ -80,6 +120,8 @@ def main() -> None:
     w.domain = "free"
     run("free_40000", w, skin=0.3)
     run("small_lanes16_3000", W.c2(N=3000), skin=0.3, small_lanes=16)
+    run_clumps("clumps_spring", K)
+    run_clumps("clumps_cundall_strack", beta, force_law="cundallstrack", material_props=props)
     ws = W.c4(n_systems=12, n_max=3000)
     eng = Engine(3, [x.desc() for x in ws], K, skin=0.2)
     try:

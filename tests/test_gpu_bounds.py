@@ -46,7 +46,7 @@ def test_checked_build_finds_no_index_out_of_range_and_changes_nothing():
     checked = engine_build.build(checked=True)
     plain = _drive(engine_build.LIB)
     got = _drive(checked)
-    assert len(plain) == 11 and set(got) == set(plain)
+    assert len(plain) == 13 and set(got) == set(plain)
     for case, rec in got.items():
         assert rec["status"] & ST_INDEX_RANGE == 0, (case, rec)
         assert rec == plain[case], case
