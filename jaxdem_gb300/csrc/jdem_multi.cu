@@ -34,6 +34,12 @@ __device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
   return v;
 }
 
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void red_release_add(unsigned int* p, unsigned int v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -45,9 +51,9 @@ __device__ __forceinline__ float4 ldc4(const float4* p) { return __ldcg(p); }
 // Grid barrier of a cooperative launch that also reduces step s's largest
 // squared drift.  Thread 0 of each block folds its warps' maxima (s_wmax)
 // into ctl->mx[s % 3] and arrives with one release add on the never-reset
-// arrival count; every block then polls the count until it reaches its
-// target (the launch's base plus gridDim.x per barrier), takes an acquire
-// fence and reads the slot.  Bounded: a block that polls max_spins times
+// arrival count; every block then polls the count with acquire loads until
+// it reaches its target (the launch's base plus gridDim.x per barrier) and
+// reads the slot.  Bounded: a block that polls max_spins times
 // records ST_BARRIER_TIMEOUT and returns false.  `extra` arrivals beyond the
 // grid's are awaited too; they never come, so extra > 0 makes every block
 // give up (the timeout path, exercised by a test through jdem_set_barrier_limit).
@@ -67,14 +73,17 @@ __device__ __forceinline__ bool grid_barrier_max(Ctl* ctl, unsigned int& target,
     target += gridDim.x;
     int ok = 1;
     unsigned int spins = 0;
-    while ((int)(ld_relaxed_u32(&ctl->bar_count) - (target + extra)) < 0) {
+    // acquire polls: the one that sees every arrival orders this block's later
+    // reads after the other blocks' released writes (a separate fence after a
+    // relaxed poll cost 0.25-0.3 us a step at 4096 spheres)
+    while ((int)(ld_acquire_u32(&ctl->bar_count) - (target + extra)) < 0) {
       if (++spins > max_spins) {
         atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
         ok = 0;
         break;
       }
     }
-    fence_acquire();
+    if (!ok) fence_acquire();
     s_ok = ok;
     s_m2 = ld_relaxed_u32(slot);
   }
