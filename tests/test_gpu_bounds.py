@@ -4,7 +4,7 @@
 list entry, list row length, cell key, sort permutation index, staged candidate index
 and stencil range the kernels index with is range-checked, and a failed check sets
 device status bit 32 and skips the access (the regular build compiles each check to
-true).  ``bounds_driver.py`` runs the engine's main paths in a child process, once
+true).  ``bounds_cases.py`` runs the engine's main paths in a child process, once
 through the regular library and once through the checked one: no case may set the bit,
 and each case's positions, velocities, forces, contacts, neighbour list and frames must
 equal the regular library's bit for bit.
@@ -35,7 +35,7 @@ def _build(built):
 
 def _drive(lib: Path) -> dict:
     env = dict(os.environ, JDEM_LIBRARY=str(lib))
-    r = subprocess.run([sys.executable, str(ROOT / "tests" / "bounds_driver.py")], env=env, capture_output=True,
+    r = subprocess.run([sys.executable, str(ROOT / "tests" / "bounds_cases.py")], env=env, capture_output=True,
                        text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-4000:]
     recs = [json.loads(line) for line in r.stdout.splitlines() if line.startswith("{")]
