@@ -64,7 +64,8 @@ def parse():
     p.add_argument("--skin", type=float, default=None)
     p.add_argument("--prune-skin", type=float, default=0.0,
                    help="inner-list margin of the Verlet-list dynamic pruning (0: skin / 3, < 0: off)")
-    p.add_argument("--brick", type=int, default=0, help="particles per list-build brick (0: 240)")
+    p.add_argument("--brick", type=int, default=0,
+                   help="particles per list-build brick (0: 240, 60 at most 32768 particles)")
     p.add_argument("--force-block", type=int, default=0, help="threads per block of k_force (0: 128)")
     p.add_argument("--small-lanes", type=int, default=0, help="lanes per slot at <= 32768 particles (0: 8)")
     p.add_argument("--n", type=int, default=None, help="override particle count (testing only)")
@@ -405,7 +406,7 @@ def run_ours(args, rank, world, dist):
                    "resorts_in_timed_region": rebuilds_timed,
                    "graphs_captured_in_timed_region": graphs_captured_timed,
                    "prune_skin": "off" if prune_skin < 0 else (prune_skin or skin / 3.0),
-                   "brick_particles": brick or 240,
+                   "brick_particles": brick or (240 if w.N > 32768 else 60),
                    "force_block": block or 128, "small_lanes": lanes or 8,
                    "prunes_in_timed_region": stats["prunes"] - prunes_before,
                    "verlet_list": {"capacity": stats["list_capacity"], "tiles": stats["list_tiles"],

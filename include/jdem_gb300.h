@@ -111,7 +111,8 @@ typedef struct {
                                    the drift since its build exceeds prune_skin / 2.
                                    0: skin / 3; < 0: off (every step walks the full list) */
   int32_t brick_particles;      /* list build: particles per brick of cells staged in shared
-                                   memory (<= 0: 240) */
+                                   memory (<= 0: 240, or 60 for handles of at most 32768
+                                   slots) */
   int32_t force_block;          /* threads per block of the fused force kernel of handles above
                                    32768 slots: 64, 128 or 256 (0: 128); results do not depend
                                    on it */

@@ -269,7 +269,7 @@ class Engine:
         cfg.force_law = FORCE_LAW[force_law]
         # inner-list margin of the dynamic pruning (0: skin / 3, < 0: off)
         cfg.prune_skin = float(prune_skin)
-        # particles per shared-memory brick of the list build (0: 240)
+        # particles per shared-memory brick of the list build (0: 240, 60 at most 32768 particles)
         cfg.brick_particles = int(brick_particles)
         # threads per block of the fused force kernel above 32768 slots (0: 128), and
         # lanes per slot of the small-system force kernels (0: 8)

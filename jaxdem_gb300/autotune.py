@@ -77,9 +77,11 @@ def workload_key(w) -> str:
 
 
 # prune skin as a fraction of the skin (-1: pruning off), list-build brick sizes,
-# force-kernel block sizes (above 32768 particles) and lanes per slot (at most 32768)
+# force-kernel block sizes (above 32768 particles) and lanes per slot and brick sizes
+# (at most 32768: few particles make few bricks, so smaller ones keep more SMs busy)
 PRUNE_CANDIDATES = (-1.0, 0.2, 1.0 / 3.0, 0.5)
 BRICK_CANDIDATES = (120, 240, 480)
+SMALL_BRICK_CANDIDATES = (30, 60, 120)
 BLOCK_CANDIDATES = (64, 128, 256)
 LANE_CANDIDATES = (4, 8, 16)
 SMALL_SLOTS = 32768
@@ -107,8 +109,8 @@ def tune_shapes(make_engine: Callable[..., "object"], upload: Callable[["object"
     ``make_engine(skin=..., prune_skin=..., brick_particles=..., force_block=..., small_lanes=...)``
     builds an engine and ``upload(engine)`` loads the state.  ``best`` holds those five
     arguments; ``timings`` the seconds per step of every candidate, per shape.  The prune
-    skin, brick size and block size only matter above 32768 particles (the fused list kernel
-    and the brick build); at most 32768 particles the skin and the lanes per slot are tuned.
+    skin and block size only matter above 32768 particles (the fused list kernel); at most
+    32768 particles the skin, the lanes per slot and the (smaller) brick sizes are tuned.
     """
     cache = _load() if use_cache else {}
     ckey = None if key is None else "shapes:" + key
@@ -120,7 +122,7 @@ def tune_shapes(make_engine: Callable[..., "object"], upload: Callable[["object"
                 c.get("timings", {}))
     timings = {"skin": {}, "prune": {}, "brick": {}, "block": {}, "lanes": {}}
     large = n_particles > SMALL_SLOTS
-    cur = {"prune_skin": 0.0, "brick_particles": 240, "force_block": 128, "small_lanes": 8}
+    cur = {"prune_skin": 0.0, "brick_particles": 240 if large else 60, "force_block": 128, "small_lanes": 8}
     for c in CANDIDATES:
         timings["skin"][str(c)] = _time_chunk(make_engine, upload, {**cur, "skin": c * rmax}, steps)
     skin_rel = float(min(timings["skin"], key=timings["skin"].get))
@@ -142,6 +144,9 @@ def tune_shapes(make_engine: Callable[..., "object"], upload: Callable[["object"
         for g in LANE_CANDIDATES:
             timings["lanes"][str(g)] = _time_chunk(make_engine, upload, {**cur, "small_lanes": g}, steps)
         cur["small_lanes"] = int(min(timings["lanes"], key=timings["lanes"].get))
+        for bk in SMALL_BRICK_CANDIDATES:
+            timings["brick"][str(bk)] = _time_chunk(make_engine, upload, {**cur, "brick_particles": bk}, steps)
+        cur["brick_particles"] = int(min(timings["brick"], key=timings["brick"].get))
     best = {"skin": cur["skin"], "prune_skin": -1.0 if prune_rel < 0 else prune_rel * cur["skin"],
             "brick_particles": cur["brick_particles"], "force_block": cur["force_block"],
             "small_lanes": cur["small_lanes"]}

@@ -155,7 +155,7 @@ int JdemHandle::setup(const JdemConfig* cfg) {
   nl_request = cfg->neighbor_list;
   if (!std::isfinite(cfg->prune_skin)) return fail(JDEM_ERR_BAD_ARG, "config: prune_skin must be finite");
   prune_req = cfg->prune_skin;
-  brick_tt = cfg->brick_particles > 0 ? (double)cfg->brick_particles : 240.0;
+  brick_tt = cfg->brick_particles > 0 ? (double)cfg->brick_particles : 0.0;  // 0: by handle size (plan_tiles)
   if (cfg->force_block != 0 && cfg->force_block != 64 && cfg->force_block != 128 && cfg->force_block != 256)
     return fail(JDEM_ERR_BAD_ARG, "config: force_block must be 0, 64, 128 or 256");
   if (cfg->small_lanes != 0 && cfg->small_lanes != 4 && cfg->small_lanes != 8 && cfg->small_lanes != 16)
@@ -399,7 +399,8 @@ int JdemHandle::plan_grid(const float* rmax_s, const float* lo_s, const float* h
 }
 
 // Tiles of the brick list build (jdem_tiles.cu) for every system: bricks of
-// cells holding about brick_tt particles (240 unless configured), near-cubic so the staged stencil region
+// cells holding about brick_tt particles (unless configured, 240, and 60 for handles of at most
+// kSmallForceSlots slots, whose few bricks would leave most SMs idle), near-cubic so the staged stencil region
 // (the brick grown by one cell per side) is small against the brick; a system
 // smaller than one brick is one tile.  Free domains re-grid on the device at
 // every re-sort, so a handle with one keeps the per-slot list build (no tiles).
@@ -407,7 +408,7 @@ int JdemHandle::plan_tiles() {
   std::vector<TileDesc> t;
   int nst = 0, nv = 0, nrows = 0;
   if (!any_free && use_nl) {
-    const double TT = brick_tt;
+    const double TT = brick_tt > 0.0 ? brick_tt : (P <= kSmallForceSlots ? 60.0 : 240.0);
     constexpr long long kMaxNV = 2048, kMaxHomeRows = 256, kMaxRows = 512;
     double stage_max = 0.0;
     long long nv_max = 0, rows_max = 0;

@@ -71,7 +71,7 @@ struct JdemHandle {
   bool use_nl = true;
   int nl_request = 0;
   float prune_req = 0.0f;  // JdemConfig.prune_skin (0: skin / 3, < 0: off)
-  double brick_tt = 240.0;  // particles per list-build brick (JdemConfig.brick_particles)
+  double brick_tt = 0.0;  // particles per list-build brick (JdemConfig.brick_particles; 0: by handle size)
   bool rot_active = false;
   bool uploaded = false;
   bool bbox_pending = false;

@@ -41,16 +41,20 @@ def test_coordinate_search_picks_each_shape_and_caches(monkeypatch, tmp_path):
     assert len(calls) == n and best2 == best
 
 
-def test_small_systems_tune_the_skin_and_lanes_per_slot(monkeypatch, tmp_path):
+def test_small_systems_tune_the_skin_lanes_per_slot_and_bricks(monkeypatch, tmp_path):
     seen = []
     monkeypatch.setattr(autotune, "_time_chunk",
-                        lambda mk, up, p, s: seen.append(p) or p["skin"] + 0.001 * abs(p["small_lanes"] - 16))
+                        lambda mk, up, p, s: seen.append(p) or p["skin"] + 0.001 * abs(p["small_lanes"] - 16)
+                        + 1e-6 * abs(p["brick_particles"] - 30))
     monkeypatch.setattr(autotune, "CACHE", tmp_path / "tune.json")
     best, timings = autotune.tune_shapes(None, None, 0.5, 4096, key=None)
-    assert len(seen) == len(autotune.CANDIDATES) + len(autotune.LANE_CANDIDATES)
+    n_lanes, n_bricks = len(autotune.LANE_CANDIDATES), len(autotune.SMALL_BRICK_CANDIDATES)
+    assert len(seen) == len(autotune.CANDIDATES) + n_lanes + n_bricks
     assert best["skin"] == min(autotune.CANDIDATES) * 0.5 and timings["prune"] == {} and timings["block"] == {}
-    assert best["small_lanes"] == 16 and best["force_block"] == 128
-    assert all(p["skin"] == best["skin"] for p in seen[-len(autotune.LANE_CANDIDATES):])
+    assert best["small_lanes"] == 16 and best["force_block"] == 128 and best["brick_particles"] == 30
+    assert all(p["brick_particles"] == 60 for p in seen[:-n_bricks])  # the small-handle default until tuned
+    assert all(p["skin"] == best["skin"] for p in seen[-(n_lanes + n_bricks):])
+    assert all(p["small_lanes"] == 16 for p in seen[-n_bricks:])
 
 
 def test_batch_tune_key_separates_batches():
