@@ -323,23 +323,24 @@ __global__ void __launch_bounds__(1024) k_scan_small(Bufs b) {
   if (threadIdx.x == 0) b.cell_start[C] = (int)b.P;
 }
 
-__global__ void k_scatter(Bufs b) {
-  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= b.P) return;
-  int key = b.key_tmp[t];
+// Slot t to its sorted position: the start of its cell plus its rank there.
+__device__ __forceinline__ void scatter_slot(const Bufs& b, long long t) {
+  const int key = b.key_tmp[t];
   if (!idx_ok(b.ctl, key, b.C)) return;
   const long long dst = (long long)b.cell_start[key] + b.slot_tmp[t];
   if (idx_ok(b.ctl, dst, b.P)) b.perm_tmp[dst] = (int)t;
 }
 
+__global__ void k_scatter(Bufs b) {
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= b.P) return;
+  scatter_slot(b, t);
+}
+
 // Per cell: order the cell's slots by original index (the stable order of
 // lax.sort([hash, iota]), cell_list.py:64) and clear the occupancy counter.
-__global__ void k_cellsort(Bufs b) {
-  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
-  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (c >= b.C) return;
-  unsigned int sel = ld_nc_u32(&b.ctl->sel);
+__device__ __forceinline__ void cell_order(const Bufs& b, unsigned int sel, long long c) {
   int a = b.cell_start[c], e = b.cell_start[c + 1];
   b.cnt[c] = 0;
   const int32_t* orig = b.orig[sel];
@@ -356,6 +357,44 @@ __global__ void k_cellsort(Bufs b) {
     }
     b.perm_tmp[j + 1] = x;
   }
+}
+
+__global__ void k_cellsort(Bufs b) {
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= b.C) return;
+  cell_order(b, ld_nc_u32(&b.ctl->sel), c);
+}
+
+// Small handles (at most kScanSmallC cells and kSortSmallP slots): the cell
+// scan, the scatter and the per-cell ordering of a re-sort as three phases of
+// one block of 1024 threads, two launches fewer per re-sort.  Each phase is
+// k_scan_small's, k_scatter's and k_cellsort's, so the sorted order is the
+// same; the block barriers between them make each phase's global writes
+// visible to the next.
+constexpr long long kSortSmallP = 32768;
+
+__global__ void __launch_bounds__(1024) k_sort_small(Bufs b) {
+  if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
+  __shared__ int sh[32];
+  const int C = (int)b.C;
+  const int per = (C + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int lo = min(C, (int)threadIdx.x * per), hi = min(C, lo + per);
+  int s = 0;
+  for (int c = lo; c < hi; ++c) s += b.cnt[c];
+  int total;
+  int off = block_excl_scan(s, sh, total);
+  for (int c = lo; c < hi; ++c) {
+    const int v = b.cnt[c];
+    b.cell_start[c] = off;
+    off += v;
+  }
+  if (threadIdx.x == 0) b.cell_start[C] = (int)b.P;
+  __syncthreads();
+  for (long long t = threadIdx.x; t < b.P; t += blockDim.x) scatter_slot(b, t);
+  __syncthreads();
+  const unsigned int sel = ld_nc_u32(&b.ctl->sel);
+  for (long long c = threadIdx.x; c < C; c += blockDim.x) cell_order(b, sel, c);
 }
 
 // Gather every slot array into the spare copy in sorted order (k_sort_fin
@@ -980,9 +1019,13 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st) {
   }
   if (dim == 3) k_bin<3><<<nblk(b.P, 256), 256, 0, st>>>(b);
   else k_bin<2><<<nblk(b.P, 256), 256, 0, st>>>(b);
-  launch_scan(b, st);
-  k_scatter<<<nblk(b.P, 256), 256, 0, st>>>(b);
-  k_cellsort<<<nblk(b.C, 256), 256, 0, st>>>(b);
+  if (b.C <= kScanSmallC && b.P <= kSortSmallP) {
+    k_sort_small<<<1, 1024, 0, st>>>(b);
+  } else {
+    launch_scan(b, st);
+    k_scatter<<<nblk(b.P, 256), 256, 0, st>>>(b);
+    k_cellsort<<<nblk(b.C, 256), 256, 0, st>>>(b);
+  }
   k_gather<<<nblk(b.P, 256), 256, 0, st>>>(b);
   k_sort_fin<<<1, 1, 0, st>>>(b.ctl);
 }
