@@ -397,8 +397,26 @@ __global__ void __launch_bounds__(1024) k_sort_small(Bufs b) {
   for (long long c = threadIdx.x; c < C; c += blockDim.x) cell_order(b, sel, c);
 }
 
+// After the gather: the sorted copies become current and the list is due.
+__device__ __forceinline__ void sort_fin(Ctl* ctl) {
+  ctl->sel ^= 1u;
+  ctl->pos_sel ^= 1u;
+  ctl->need_rebuild = 0u;
+  ctl->nl_dirty = 1u;
+  ctl->bound = 0.0f;
+  ctl->rebuilds += 1u;
+}
+
+__global__ void k_sort_fin(Ctl* ctl) {
+  if (ctl->need_rebuild == 0u) return;
+  sort_fin(ctl);
+}
+
 // Gather every slot array into the spare copy in sorted order (k_sort_fin
 // then flips the copies).
+// FLIP (small handles, a few blocks): the last block to finish flips the
+// copies itself, one launch fewer per re-sort.
+template <bool FLIP>
 __global__ void k_gather(Bufs b) {
   if (ld_nc_u32(&b.ctl->need_rebuild) == 0u) return;
   long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -437,18 +455,19 @@ __global__ void k_gather(Bufs b) {
     b.orig[sel ^ 1u][u] = __ldcs(&b.orig[sel][t]);
     b.key[sel ^ 1u][u] = __ldcs(&b.key_tmp[t]);
   }
+  if (FLIP) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (atomicAdd(&b.ctl->gather_done, 1u) == gridDim.x - 1u) {
+        __threadfence();
+        b.ctl->gather_done = 0u;
+        sort_fin(b.ctl);
+      }
+    }
+  }
 }
 
-// After k_gather: the sorted copies become current and the list is due.
-__global__ void k_sort_fin(Ctl* ctl) {
-  if (ctl->need_rebuild == 0u) return;
-  ctl->sel ^= 1u;
-  ctl->pos_sel ^= 1u;
-  ctl->need_rebuild = 0u;
-  ctl->nl_dirty = 1u;
-  ctl->bound = 0.0f;
-  ctl->rebuilds += 1u;
-}
 
 // ------------------------------------------------------------ first drift
 
@@ -1026,8 +1045,12 @@ void launch_rebuild(int dim, const Bufs& b, bool any_free, cudaStream_t st) {
     k_scatter<<<nblk(b.P, 256), 256, 0, st>>>(b);
     k_cellsort<<<nblk(b.C, 256), 256, 0, st>>>(b);
   }
-  k_gather<<<nblk(b.P, 256), 256, 0, st>>>(b);
-  k_sort_fin<<<1, 1, 0, st>>>(b.ctl);
+  if (b.P <= kSortSmallP) {
+    k_gather<true><<<nblk(b.P, 256), 256, 0, st>>>(b);
+  } else {
+    k_gather<false><<<nblk(b.P, 256), 256, 0, st>>>(b);
+    k_sort_fin<<<1, 1, 0, st>>>(b.ctl);
+  }
 }
 
 void launch_pre(int dim, const Bufs& b, int mode, cudaStream_t st) {
